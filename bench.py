@@ -1,0 +1,272 @@
+"""Benchmark of the DynEarthSol3D explicit time step on one GB300.
+
+A "step" is one iteration of the reference's loop body (dynearthsol.cxx:358-394)
+over the whole mesh.  The workload is config 2: 200x200x40 hexes x 6 =
+9,600,000 tetrahedra (1,656,441 nodes), elasto-plastic, FP64 plain form.  The
+state (about 4.8 GB) is far larger than the 129 MB L2, so no flush is needed
+between timed steps.
+
+  python bench.py [--gpus 1] [--steps K] [--warmup W] [--config 2] [--impl ours|reference]
+
+--impl reference times the CPU implementation of the same loop (the oracle
+restatement, OpenMP on every host core; the reference's own objects are only
+available in the build container) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "dynearthsol-old_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "element-steps/s on 1 GB300: FP64 plain vs FP32+MLP closure at stated error, %HBM"
+UNIT = "element-steps/s"
+# compulsory bytes per element-step of the FP64 elasto-plastic step: stress,
+# strain (6 x 8 B read + write each), plastic strain (read + write), connectivity;
+# nodal coord, vel (read + write), T (read + write), bcflag, scaled by nodes/elements
+B_ELEM = 6 * 8 * 2 * 2 + 8 * 2 + 4 * 4
+B_NODE = 3 * 8 * 2 * 2 + 8 * 2 + 4
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index=0):
+        self.samples, self.proc, self.index = [], None, index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit())
+        mx = max(float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 4 + i and s[4 + i].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def build_case(cfg_key):
+    import des_gb300 as D
+    from des_gb300 import workload as W
+    cfg = W.CONFIGS[cfg_key]
+    mesh, p, T, pls, topo = D.setup_case(cfg)
+    return cfg, mesh, p, T, pls
+
+
+def cpu_baseline(cfg_key, steps=3, warmup=1):
+    """The CPU restatement (OpenMP, all host threads) on a bounded sample:
+    `steps` timed iterations of the full workload after `warmup`."""
+    from des_gb300 import workload as W
+    from oracle.oracle import PortOracle
+    cfg, mesh, p, T, pls = build_case(cfg_key)
+    o = PortOracle(mesh, p)
+    s = W.new_state(mesh, T, pls)
+    o.init_fields(s)
+    if warmup:
+        o.step(s, warmup)
+    t0 = time.perf_counter()
+    o.step(s, steps)
+    dt = time.perf_counter() - t0
+    from oracle.oracle import PortOracle as PO
+    threads = PO.lib().dso_num_threads()
+    return {"value": mesh.nelem * steps / dt, "unit": UNIT, "cores": int(threads), "kind": "port",
+            "sample": f"{steps} steps of {cfg.name} ({mesh.nelem} tets) after {warmup} warm-up, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    # bounded sample: at most 5 timed steps of the full mesh after 1 warm-up step
+    steps = min(args.steps, 5)
+    cb = cpu_baseline(args.config, steps=steps, warmup=1)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+            "n_gpus": args.gpus, "steps": steps, "warmup": 1,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "config2_ep_200x200x40 (9.6M tets)"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import numpy as np
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local)
+        tdist.init_process_group("nccl")
+
+    D.build()
+    cfg, mesh, p, T, pls = build_case(args.config)
+    dev = D.Device(mesh, p, device=local)
+    s = W.new_state(mesh, T, pls)
+    dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+    dev.init_fields()
+    dev.step(args.warmup)                       # warm-up (also captures the graph)
+
+    def barrier():
+        if dist:
+            tdist.barrier()
+
+    barrier()
+    with ClockSampler(local) as clk:
+        ms = dev.time_steps(args.steps)
+    barrier()
+    if dist:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+    rep = dev.report()
+    value = world * mesh.nelem * args.steps / (ms / 1e3)
+
+    # per-pass device times over extra steps (same arithmetic, launched one by one)
+    prof_steps = max(2, min(args.steps, 5))
+    per_pass = dev.profile_steps(prof_steps)
+    names = ["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"]
+    top = int(np.argmax(per_pass))
+    # algorithmic bytes per element of each pass (each array it must read or
+    # write once; nodal arrays scaled by nodes/elements)
+    r = mesh.nnode / mesh.nelem
+    alg = {
+        "N-A": r * (8 * 2 + 8 * 3) + 4 * 4 * 0,
+        "E-B": 6 * 8 * 3 + 6 * 8 * 3 + 8 * 2 + 8 * 5 + 16,
+        "N-B": r * 8 * 2 + 8,
+        "E-C": 6 * 8 * 2 + 12 * 8 + 12 * 8 + 8 * 3 + 16,
+        "N-C": r * (3 * 8 * 5 + 8 + 4) + 12 * 8,
+        "E-A": 16 + 8 * 3 + 12 * 8 + 6 * 8 * 4 + 6 * 8 + 8 * 7,
+    }
+    hbm, hbm_kind = peaks()
+    t_top = per_pass[top] / prof_steps / 1e3
+    achieved = alg[names[top]] * mesh.nelem / t_top / 1e9
+    step_alg = (B_ELEM + B_NODE * r) * mesh.nelem
+    step_gbs = step_alg / (ms / args.steps / 1e3) / 1e9
+
+    # end to end through the drop-in entry point with pinned host buffers:
+    # every step uploads the loop's state from the host and downloads it back
+    host = abi.State(mesh.nnode, mesh.nelem)
+    dev.download(host, abi.F_ALL)
+    D.pin(host)
+    mask = abi.F_STEP_STATE
+    nb = {abi.F_COORD: 24 * mesh.nnode, abi.F_VEL: 24 * mesh.nnode, abi.F_FORCE: 24 * mesh.nnode,
+          abi.F_TEMPERATURE: 8 * mesh.nnode, abi.F_MASS: 24 * mesh.nnode,
+          abi.F_NTMP: 8 * mesh.nnode, abi.F_VOLUME: 16 * mesh.nelem,
+          abi.F_STRESS: 48 * mesh.nelem, abi.F_STRAIN: 48 * mesh.nelem,
+          abi.F_STRAIN_RATE: 48 * mesh.nelem, abi.F_PLSTRAIN: 16 * mesh.nelem,
+          abi.F_DPRESSURE: 8 * mesh.nelem, abi.F_EDVOLDT: 8 * mesh.nelem,
+          abi.F_SHAPE: 96 * mesh.nelem, abi.F_SCALARS: 0}
+    io_bytes = sum(v for k, v in nb.items() if mask & k)
+    e2e_steps = max(1, min(args.steps, 5))
+    dev.step_host(host, 1, mask)                # warm-up of the host path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dev.step_host(host, 1, mask)
+    e2e_s = time.perf_counter() - t0
+    D.unpin(host)
+    e2e = world * mesh.nelem * e2e_steps / e2e_s
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(args.config, steps=2, warmup=1)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{cfg.name}: {mesh.nelem} tets / {mesh.nnode} nodes, "
+                               "elasto-plastic, FP64 plain form",
+                   "parallelism": f"replicas{world}", "l2": "state 4.8 GB >> 129 MB L2, no flush"},
+        "gpu_launches": dev.kernels_per_step * args.steps,
+        "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "peak_kind": hbm_kind,
+                     "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,
+                     "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm},
+        "passes_ms_per_step": {n: t / prof_steps for n, t in zip(names, per_pass)},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
+                "d2h_bytes_per_step": io_bytes},
+        "clocks": clk.summary(),
+        "status": rep.status, "eigen_solves": rep.eigen_solves,
+        "device_gb": dev.device_bytes / 1e9,
+    }
+    if cb:
+        line["cpu_baseline"] = cb
+    dev.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        tdist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", default="2")
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,889 @@
+// C ABI of the GB300 time-step library: device state, upload/download, the
+// per-function entry points and the captured whole-step graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "des_gpu.h"
+#include "des_kernels.cuh"
+
+using namespace des;
+
+namespace {
+
+const int kElemBlock = 128;
+const int kNodeBlock = 256;
+const int kStepKernels = 6;
+
+inline int blocks(long long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+struct des_gpu {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nnode = 0, nelem = 0, nmat = 0;
+    des_params P;
+    Consts hK;
+    std::vector<std::vector<int>> mix_counts;
+    Dev d;
+    Consts *dK = nullptr;
+    Clock *dclk = nullptr;
+    std::vector<void *> allocs;
+    long long bytes = 0;
+    double *staging = nullptr;
+    long long staging_elems = 0;
+    cudaGraphExec_t graph = nullptr;
+    bool primed = false;
+    bool stress_bcs = false;
+    int bfacets_count[DES_NBDRY] = {0};
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? DES_OK : DES_ERR_CUDA; }
+#define DES_CUDA(call)                          \
+    do {                                        \
+        cudaError_t _e = (call);                \
+        if (_e != cudaSuccess) return DES_ERR_CUDA; \
+    } while (0)
+#define DES_LAUNCH()                                        \
+    do {                                                    \
+        if (cudaGetLastError() != cudaSuccess) return DES_ERR_CUDA; \
+    } while (0)
+
+template <class T>
+int dev_alloc(des_gpu *g, T **p, size_t n)
+{
+    void *q = nullptr;
+    size_t bytes = sizeof(T) * (n ? n : 1);
+    if (cudaMalloc(&q, bytes) != cudaSuccess) return DES_ERR_NOMEM;
+    g->allocs.push_back(q);
+    g->bytes += (long long)bytes;
+    if (cudaMemset(q, 0, bytes) != cudaSuccess) return DES_ERR_CUDA;
+    *p = static_cast<T *>(q);
+    return DES_OK;
+}
+
+double mv(const des_matvec &v, int m) { return v.len == 1 ? v.v[0] : v.v[m]; }
+
+// matprops.cxx:436-461
+double arith_mean(const des_matvec &s, const std::vector<int> &n)
+{
+    if (s.len == 1) return s.v[0];
+    double result = 0;
+    int m = 0;
+    for (int i = 0; i < s.len; i++) {
+        result += n[i] * s.v[i];
+        m += n[i];
+    }
+    return result / m;
+}
+double harm_mean(const des_matvec &s, const std::vector<int> &n)
+{
+    if (s.len == 1) return s.v[0];
+    double result = 0;
+    int m = 0;
+    for (int i = 0; i < s.len; i++) {
+        result += n[i] / s.v[i];
+        m += n[i];
+    }
+    return m / result;
+}
+
+int check_params(const des_params &p, int nmat)
+{
+    if (p.nmat != nmat || nmat < 1 || nmat > DES_MAX_MAT) return DES_ERR_ARG;
+    if (p.is_plane_strain) return DES_ERR_UNSUPPORTED;
+    if (p.surface_process_option != 0) return DES_ERR_UNSUPPORTED;
+    if (p.rheol_type != DES_RH_ELASTIC && p.rheol_type != DES_RH_VISCOUS &&
+        p.rheol_type != DES_RH_MAXWELL && p.rheol_type != DES_RH_EP && p.rheol_type != DES_RH_EVP)
+        return DES_ERR_OPTION;
+    if (p.damping_option < 0 || p.damping_option > 4) return DES_ERR_OPTION;
+    if (p.ref_pressure_option != 0 && p.gravity != 0) return DES_ERR_UNSUPPORTED;
+    if (p.precision != DES_PREC_FP64) return DES_ERR_UNSUPPORTED;
+    const des_matvec *vs[] = {&p.rho0, &p.alpha, &p.bulk_modulus, &p.shear_modulus,
+                              &p.visc_exponent, &p.visc_coefficient, &p.visc_activation_energy,
+                              &p.heat_capacity, &p.therm_cond, &p.pls0, &p.pls1, &p.cohesion0,
+                              &p.cohesion1, &p.friction_angle0, &p.friction_angle1,
+                              &p.dilation_angle0, &p.dilation_angle1};
+    for (const des_matvec *v : vs)
+        if (!(v->len == nmat || (v->len == 1 && nmat != 1) || (v->len == 1 && nmat == 1)))
+            return DES_ERR_TOPOLOGY;   // VectorBase::create rejects it (matprops.cxx:509-520)
+    return DES_OK;
+}
+
+// Consts from params and the distinct marker-count vectors
+int build_consts(des_gpu *g)
+{
+    const des_params &p = g->P;
+    Consts &K = g->hK;
+    std::memset(&K, 0, sizeof(K));
+    MatTable &M = K.M;
+    M.nmat = g->nmat;
+    M.nmix = (int)g->mix_counts.size();
+    const double gas_constant = 8.3144;
+    for (int m = 0; m < g->nmat; ++m) {
+        M.rho0[m] = mv(p.rho0, m);
+        M.alpha[m] = mv(p.alpha, m);
+        double ve = mv(p.visc_exponent, m);
+        M.vexp_pw[m] = 1 / ve - 1;
+        M.vexp_pw1[m] = -1 / ve;
+        M.vcoef_pow[m] = std::pow(0.75 * mv(p.visc_coefficient, m), M.vexp_pw1[m]);
+        M.vQ[m] = mv(p.visc_activation_energy, m);
+        M.vnR[m] = ve * gas_constant;
+        M.pls0[m] = mv(p.pls0, m);
+        M.pls1[m] = mv(p.pls1, m);
+        M.c0[m] = mv(p.cohesion0, m);
+        M.c1[m] = mv(p.cohesion1, m);
+        M.f0[m] = mv(p.friction_angle0, m);
+        M.f1[m] = mv(p.friction_angle1, m);
+        M.d0[m] = mv(p.dilation_angle0, m);
+        M.d1[m] = mv(p.dilation_angle1, m);
+        M.hslope[m] = (M.c1[m] - M.c0[m]) / (M.pls1[m] - M.pls0[m]);
+    }
+    const double deg2rad = 3.1415926535897932384626433832795 / 180;
+    M.phi_c = M.f0[0];
+    double sphi = std::sin(M.phi_c * deg2rad);
+    M.sphi_c = sphi;
+    M.anphi_c = (1 + sphi) / (1 - sphi);
+    M.sqanphi_c = std::sqrt(M.anphi_c);
+    M.tphi_c = std::tan(M.phi_c * deg2rad);
+    M.psi_c = M.d0[0];
+    double spsi = std::sin(M.psi_c * deg2rad);
+    M.spsi_c = spsi;
+    M.anpsi_c = (1 + spsi) / (1 - spsi);
+    M.visc_min = p.visc_min;
+    M.visc_max = p.visc_max;
+    M.tension_max = p.tension_max;
+    double pseudo_speed = p.max_vbc_val * p.inertial_scaling;
+    for (int i = 0; i < M.nmix; ++i) {
+        const std::vector<int> &cnt = g->mix_counts[i];
+        Mix &x = M.mix[i];
+        x.bulkm = harm_mean(p.bulk_modulus, cnt);
+        x.shearm = harm_mean(p.shear_modulus, cnt);
+        x.cp = arith_mean(p.heat_capacity, cnt);
+        x.k = arith_mean(p.therm_cond, cnt);
+        x.rho_qs = x.bulkm / (pseudo_speed * pseudo_speed);
+        x.dt_maxwell = 0.5 * p.visc_min / (1e-40 + x.shearm);
+        int n = 0, nonzero = 0, which = -1;
+        for (int m = 0; m < g->nmat; ++m) {
+            x.count[m] = cnt[m];
+            n += cnt[m];
+            if (cnt[m] != 0) {
+                ++nonzero;
+                which = m;
+            }
+        }
+        x.n = n;
+        bool pow2 = which >= 0 && (cnt[which] & (cnt[which] - 1)) == 0;
+        x.single = (nonzero == 1 && pow2) ? which : -1;
+    }
+    K.gravity = p.gravity;
+    K.damping_factor = p.damping_factor;
+    K.surface_temperature = p.surface_temperature;
+    K.dt_fraction = p.dt_fraction;
+    K.fixed_dt = p.fixed_dt;
+    K.inertial_scaling = p.inertial_scaling;
+    K.max_vbc_val = p.max_vbc_val;
+    K.therm_diff_max = p.therm_diff_max;
+    K.zlength = p.zlength;
+    K.rho0_0 = p.rho0.v[0];
+    K.compensation_pressure = p.compensation_pressure;
+    K.damping_option = p.damping_option;
+    K.is_qs = p.is_quasi_static ? 1 : 0;
+    K.thermal = p.has_thermal_diffusion ? 1 : 0;
+    K.rheol = p.rheol_type;
+    for (int i = 0; i < DES_NBDRY; ++i) {
+        K.vbc_types[i] = p.vbc_types[i];
+        K.vbc_values[i] = p.vbc_values[i];
+        for (int k = 0; k < 3; ++k) K.bnormals[i][k] = p.bnormals[i][k];
+        for (int j = 0; j < DES_NBDRY; ++j)
+            for (int k = 0; k < 3; ++k) K.edge[i][j][k] = p.edge_vectors[i][j][k];
+    }
+    // apply_stress_bcs (bc.cxx:503-595) does something only for these cases
+    g->stress_bcs = false;
+    if (p.gravity != 0) {
+        for (int i = 0; i < DES_NBDRY; ++i) {
+            int t = p.vbc_types[i];
+            if (t != 0 && t != 2 && t != 4) continue;
+            if (i == 4 && !p.has_winkler_foundation) continue;
+            if (i == 5 && !p.has_water_loading) continue;
+            if (g->bfacets_count[i] > 0) g->stress_bcs = true;
+        }
+    }
+    if (p.has_elastic_foundation) g->stress_bcs = true;
+    if (cudaMemcpyAsync(g->dK, &g->hK, sizeof(Consts), cudaMemcpyHostToDevice, g->stream) !=
+        cudaSuccess)
+        return DES_ERR_CUDA;
+    return cudaStreamSynchronize(g->stream) == cudaSuccess ? DES_OK : DES_ERR_CUDA;
+}
+
+// ---- host <-> device field transfers --------------------------------------
+int upload_field(des_gpu *g, const double *host, double *dst, int ncomp, long long rows)
+{
+    if (!host) return DES_ERR_ARG;
+    long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
+    for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
+        long long nr = std::min(chunk_rows, rows - r0);
+        DES_CUDA(cudaMemcpyAsync(g->staging, host + r0 * ncomp, sizeof(double) * nr * ncomp,
+                                 cudaMemcpyHostToDevice, g->stream));
+        k_aos_to_soa<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(g->staging, dst, ncomp, nr, r0,
+                                                                       rows);
+        DES_LAUNCH();
+    }
+    return DES_OK;
+}
+int download_field(des_gpu *g, double *host, const double *src, int ncomp, long long rows)
+{
+    if (!host) return DES_ERR_ARG;
+    long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
+    for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
+        long long nr = std::min(chunk_rows, rows - r0);
+        k_soa_to_aos<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(src, g->staging, ncomp, nr, r0,
+                                                                       rows);
+        DES_LAUNCH();
+        DES_CUDA(cudaMemcpyAsync(host + r0 * ncomp, g->staging, sizeof(double) * nr * ncomp,
+                                 cudaMemcpyDeviceToHost, g->stream));
+    }
+    return DES_OK;
+}
+
+int read_clock(des_gpu *g, Clock &c)
+{
+    DES_CUDA(cudaMemcpyAsync(&c, g->dclk, sizeof(Clock), cudaMemcpyDeviceToHost, g->stream));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    return DES_OK;
+}
+
+// nodal masses current and fused-pass priming invalidated before a
+// per-function call
+int begin_fn(des_gpu *g)
+{
+    if (!g) return DES_ERR_ARG;
+    Clock c;
+    int rc = read_clock(g, c);
+    if (rc) return rc;
+    if (!c.mass_valid) {
+        k_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
+        DES_LAUNCH();
+    }
+    g->primed = false;
+    return DES_OK;
+}
+
+int finish(des_gpu *g)
+{
+    DES_CUDA(cudaGetLastError());
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    return DES_OK;
+}
+
+int capture_step_graph(des_gpu *g)
+{
+    const Dev &d = g->d;
+    cudaGraph_t graph;
+    DES_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
+    const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
+    k_fn_a<<<nb, kNodeBlock, 0, g->stream>>>(d);
+    k_fe_b<<<eb, kElemBlock, 0, g->stream>>>(d);
+    k_sg_gather<<<nb, kNodeBlock, 0, g->stream>>>(d);
+    k_fe_c<<<eb, kElemBlock, 0, g->stream>>>(d);
+    k_fn_c<<<nb, kNodeBlock, 0, g->stream>>>(d);
+    k_fe_a<<<eb, kElemBlock, 0, g->stream>>>(d);
+    cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
+    if (e != cudaSuccess) return DES_ERR_CUDA;
+    e = cudaGraphInstantiate(&g->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    return cuda_rc(e);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *des_gpu_error_string(int code)
+{
+    switch (code) {
+    case DES_OK: return "ok";
+    case DES_ERR_OPTION: return "unknown rheology or option";
+    case DES_ERR_ARG: return "bad argument";
+    case DES_ERR_CUDA: return "CUDA runtime error";
+    case DES_ERR_NOMEM: return "device allocation failed";
+    case DES_ERR_UNSUPPORTED: return "option not supported by this library";
+    case DES_ERR_SIZE: return "size above the entry point's limit";
+    case DES_ERR_DT: return "dt <= 0";
+    case DES_ERR_TOPOLOGY: return "inconsistent mesh topology";
+    default: return "unknown error";
+    }
+}
+
+int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_gpu **out)
+{
+    if (!m || !p || !out || !m->elemmarkers) return DES_ERR_ARG;
+    int rc = check_params(*p, m->nmat);
+    if (rc) return rc;
+    des_topology *topo = nullptr;
+    rc = des_topology_build(m, &topo);
+    if (rc) return rc;
+    des_gpu *g = new (std::nothrow) des_gpu;
+    if (!g) {
+        des_topology_free(topo);
+        return DES_ERR_NOMEM;
+    }
+    if (device >= 0 && cudaSetDevice(device) != cudaSuccess) {
+        des_topology_free(topo);
+        delete g;
+        return DES_ERR_CUDA;
+    }
+    cudaGetDevice(&g->device);
+    g->P = *p;
+    g->nnode = m->nnode;
+    g->nelem = m->nelem;
+    g->nmat = m->nmat;
+    for (int i = 0; i < DES_NBDRY; ++i) g->bfacets_count[i] = topo->bfacets_count[i];
+
+    // distinct marker-count vectors ("mixes") and the element -> mix map
+    std::vector<unsigned char> mix(m->nelem);
+    {
+        std::map<std::vector<int>, int> ids;
+        std::vector<int> prev, cur(m->nmat);
+        int prev_id = -1;
+        for (int e = 0; e < m->nelem; ++e) {
+            const int *c = m->elemmarkers + (size_t)m->nmat * e;
+            cur.assign(c, c + m->nmat);
+            int n = 0;
+            for (int k = 0; k < m->nmat; ++k) n += cur[k];
+            if (n <= 0) {
+                des_topology_free(topo);
+                delete g;
+                return DES_ERR_TOPOLOGY;   // MarkerSet rejects an element without markers
+            }
+            if (prev_id >= 0 && cur == prev) {
+                mix[e] = (unsigned char)prev_id;
+                continue;
+            }
+            auto it = ids.find(cur);
+            int id;
+            if (it == ids.end()) {
+                id = (int)ids.size();
+                if (id >= kMaxMix) {
+                    des_topology_free(topo);
+                    delete g;
+                    return DES_ERR_SIZE;
+                }
+                ids[cur] = id;
+                g->mix_counts.push_back(cur);
+            } else {
+                id = it->second;
+            }
+            mix[e] = (unsigned char)id;
+            prev = cur;
+            prev_id = id;
+        }
+    }
+
+    auto fail = [&](int code) {
+        des_topology_free(topo);
+        des_gpu_destroy(g);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(DES_ERR_CUDA);
+    const size_t N = m->nnode, E = m->nelem;
+    Dev &d = g->d;
+    d.nnode = m->nnode;
+    d.nelem = m->nelem;
+    double *coord, *vel, *force, *coord0;
+    int4 *conn;
+    int *sup_off;
+    unsigned *sup_ent, *bcflag;
+    unsigned char *dmix;
+    if ((rc = dev_alloc(g, &coord, 3 * N)) || (rc = dev_alloc(g, &vel, 3 * N)) ||
+        (rc = dev_alloc(g, &force, 3 * N)) || (rc = dev_alloc(g, &coord0, 3 * N)) ||
+        (rc = dev_alloc(g, &d.T, N)) || (rc = dev_alloc(g, &d.mass, N)) ||
+        (rc = dev_alloc(g, &d.tmass, N)) || (rc = dev_alloc(g, &d.vol_n, N)) ||
+        (rc = dev_alloc(g, &d.ntmp, N)) || (rc = dev_alloc(g, &bcflag, N)) ||
+        (rc = dev_alloc(g, &sup_off, N + 1)) || (rc = dev_alloc(g, &sup_ent, 4 * E)) ||
+        (rc = dev_alloc(g, &conn, E)) || (rc = dev_alloc(g, &dmix, E)) ||
+        (rc = dev_alloc(g, &d.vol, E)) || (rc = dev_alloc(g, &d.vol_old, E)) ||
+        (rc = dev_alloc(g, &d.edvoldt, E)) || (rc = dev_alloc(g, &d.pls, E)) ||
+        (rc = dev_alloc(g, &d.dpls, E)) || (rc = dev_alloc(g, &d.dp, E)) ||
+        (rc = dev_alloc(g, &d.tmp_sg, E)) || (rc = dev_alloc(g, &d.stress, 6 * E)) ||
+        (rc = dev_alloc(g, &d.strain, 6 * E)) || (rc = dev_alloc(g, &d.srate, 6 * E)) ||
+        (rc = dev_alloc(g, &d.srate_next, 6 * E)) || (rc = dev_alloc(g, &d.shp, 12 * E)) ||
+        (rc = dev_alloc(g, &d.tmp, 12 * E)) || (rc = dev_alloc(g, &d.c_mass, E)) ||
+        (rc = dev_alloc(g, &d.c_tmass, E)) || (rc = dev_alloc(g, &d.c_trdv, E)) ||
+        (rc = dev_alloc(g, &g->dK, 1)) || (rc = dev_alloc(g, &g->dclk, 1)))
+        return fail(rc);
+    g->staging_elems = std::min<long long>(12LL * (long long)E, 1LL << 25);
+    g->staging_elems = std::max<long long>(g->staging_elems, 3LL * (long long)N < (1LL << 25) ? 3LL * (long long)N : (1LL << 25));
+    if ((rc = dev_alloc(g, &g->staging, (size_t)g->staging_elems))) return fail(rc);
+    d.x = coord; d.y = coord + N; d.z = coord + 2 * N;
+    d.vx = vel; d.vy = vel + N; d.vz = vel + 2 * N;
+    d.fx = force; d.fy = force + N; d.fz = force + 2 * N;
+    d.x0 = coord0; d.y0 = coord0 + N; d.z0 = coord0 + 2 * N;
+    d.conn = conn;
+    d.sup_off = sup_off;
+    d.sup_ent = sup_ent;
+    d.bcflag = bcflag;
+    d.mix = dmix;
+    d.K = g->dK;
+    d.clk = g->dclk;
+
+    std::vector<unsigned> ent(4 * E);
+    for (size_t q = 0; q < 4 * E; ++q)
+        ent[q] = ((unsigned)topo->support_elems[q] << 2) | (unsigned)topo->support_slots[q];
+    if (cudaMemcpy(conn, m->connectivity, sizeof(int) * 4 * E, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(sup_off, topo->support_offsets, sizeof(int) * (N + 1), cudaMemcpyHostToDevice) ||
+        cudaMemcpy(sup_ent, ent.data(), sizeof(unsigned) * 4 * E, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(bcflag, topo->bcflag, sizeof(unsigned) * N, cudaMemcpyHostToDevice) ||
+        cudaMemcpy(dmix, mix.data(), E, cudaMemcpyHostToDevice))
+        return fail(DES_ERR_CUDA);
+    des_topology_free(topo);
+    topo = nullptr;
+    Clock c0;
+    std::memset(&c0, 0, sizeof(c0));
+    c0.minl = ~0ULL;
+    c0.dtdiff = ~0ULL;
+    if (cudaMemcpy(g->dclk, &c0, sizeof(Clock), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(DES_ERR_CUDA);
+    if ((rc = build_consts(g))) return fail(rc);
+    *out = g;
+    return DES_OK;
+}
+
+int des_gpu_destroy(des_gpu *g)
+{
+    if (!g) return DES_OK;
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    for (void *p : g->allocs) cudaFree(p);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    delete g;
+    return DES_OK;
+}
+
+int des_gpu_set_params(des_gpu *g, const des_params *p)
+{
+    if (!g || !p) return DES_ERR_ARG;
+    int rc = check_params(*p, g->nmat);
+    if (rc) return rc;
+    g->P = *p;
+    g->primed = false;
+    return build_consts(g);
+}
+
+long long des_gpu_device_bytes(const des_gpu *g) { return g ? g->bytes : 0; }
+int des_gpu_kernels_per_step(const des_gpu *g) { return g ? kStepKernels : 0; }
+
+int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
+{
+    if (!g || !h || h->nnode != g->nnode || h->nelem != g->nelem) return DES_ERR_ARG;
+    if (mask & ~(unsigned)DES_F_ALL) return DES_ERR_ARG;
+    const long long N = g->nnode, E = g->nelem;
+    Dev &d = g->d;
+    int rc = DES_OK;
+#define UP(flag, ptr, dst, nc, rows) \
+    if ((mask & (flag)) && (rc = upload_field(g, h->ptr, dst, nc, rows))) return rc;
+    UP(DES_F_COORD, coord, d.x, 3, N)
+    UP(DES_F_COORD0, coord0, d.x0, 3, N)
+    UP(DES_F_VEL, vel, d.vx, 3, N)
+    UP(DES_F_FORCE, force, d.fx, 3, N)
+    UP(DES_F_TEMPERATURE, temperature, d.T, 1, N)
+    UP(DES_F_MASS, mass, d.mass, 1, N)
+    UP(DES_F_MASS, tmass, d.tmass, 1, N)
+    UP(DES_F_MASS, volume_n, d.vol_n, 1, N)
+    UP(DES_F_NTMP, ntmp, d.ntmp, 1, N)
+    UP(DES_F_VOLUME, volume, d.vol, 1, E)
+    UP(DES_F_VOLUME, volume_old, d.vol_old, 1, E)
+    UP(DES_F_STRESS, stress, d.stress, 6, E)
+    UP(DES_F_STRAIN, strain, d.strain, 6, E)
+    UP(DES_F_STRAIN_RATE, strain_rate, d.srate, 6, E)
+    UP(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
+    UP(DES_F_PLSTRAIN, delta_plstrain, d.dpls, 1, E)
+    UP(DES_F_DPRESSURE, dpressure, d.dp, 1, E)
+    UP(DES_F_EDVOLDT, edvoldt, d.edvoldt, 1, E)
+    UP(DES_F_SHAPE, shpdx, d.shp, 4, E)
+    UP(DES_F_SHAPE, shpdy, d.shp + 4 * E, 4, E)
+    UP(DES_F_SHAPE, shpdz, d.shp + 8 * E, 4, E)
+    UP(DES_F_TMP_RESULT, tmp_result, d.tmp, 12, E)
+    UP(DES_F_TMP_RESULT, tmp_result_sg, d.tmp_sg, 1, E)
+#undef UP
+    if (mask & (DES_F_SCALARS | DES_F_MASS)) {
+        Clock c;
+        if ((rc = read_clock(g, c))) return rc;
+        if (mask & DES_F_SCALARS) {
+            c.time = h->time;
+            c.dt = h->dt;
+            c.steps = h->steps;
+        }
+        if (mask & DES_F_MASS) c.mass_valid = 1;
+        k_clock_set<<<1, 32, 0, g->stream>>>(g->dclk, c.time, c.dt, c.steps, c.mass_valid);
+        DES_LAUNCH();
+    }
+    g->primed = false;
+    return finish(g);
+}
+
+int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
+{
+    if (!g || !h || h->nnode != g->nnode || h->nelem != g->nelem) return DES_ERR_ARG;
+    if (mask & ~(unsigned)DES_F_ALL) return DES_ERR_ARG;
+    const long long N = g->nnode, E = g->nelem;
+    Dev &d = g->d;
+    Clock c;
+    int rc = read_clock(g, c);
+    if (rc) return rc;
+    if ((mask & DES_F_MASS) && !c.mass_valid) {
+        k_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(d);
+        DES_LAUNCH();
+    }
+#define DOWN(flag, ptr, src, nc, rows) \
+    if ((mask & (flag)) && (rc = download_field(g, h->ptr, src, nc, rows))) return rc;
+    DOWN(DES_F_COORD, coord, d.x, 3, N)
+    DOWN(DES_F_COORD0, coord0, d.x0, 3, N)
+    DOWN(DES_F_VEL, vel, d.vx, 3, N)
+    DOWN(DES_F_FORCE, force, d.fx, 3, N)
+    DOWN(DES_F_TEMPERATURE, temperature, d.T, 1, N)
+    DOWN(DES_F_MASS, mass, d.mass, 1, N)
+    DOWN(DES_F_MASS, tmass, d.tmass, 1, N)
+    DOWN(DES_F_MASS, volume_n, d.vol_n, 1, N)
+    DOWN(DES_F_NTMP, ntmp, d.ntmp, 1, N)
+    DOWN(DES_F_VOLUME, volume, d.vol, 1, E)
+    DOWN(DES_F_VOLUME, volume_old, d.vol_old, 1, E)
+    DOWN(DES_F_STRESS, stress, d.stress, 6, E)
+    DOWN(DES_F_STRAIN, strain, d.strain, 6, E)
+    DOWN(DES_F_STRAIN_RATE, strain_rate, d.srate, 6, E)
+    DOWN(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
+    DOWN(DES_F_PLSTRAIN, delta_plstrain, d.dpls, 1, E)
+    DOWN(DES_F_DPRESSURE, dpressure, d.dp, 1, E)
+    DOWN(DES_F_EDVOLDT, edvoldt, d.edvoldt, 1, E)
+    DOWN(DES_F_SHAPE, shpdx, d.shp, 4, E)
+    DOWN(DES_F_SHAPE, shpdy, d.shp + 4 * E, 4, E)
+    DOWN(DES_F_SHAPE, shpdz, d.shp + 8 * E, 4, E)
+    DOWN(DES_F_TMP_RESULT, tmp_result, d.tmp, 12, E)
+    DOWN(DES_F_TMP_RESULT, tmp_result_sg, d.tmp_sg, 1, E)
+#undef DOWN
+    if (mask & DES_F_SCALARS) {
+        h->time = c.time;
+        h->dt = c.dt;
+        h->steps = c.steps;
+    }
+    return finish(g);
+}
+
+int des_gpu_report(des_gpu *g, des_step_report *r)
+{
+    if (!g || !r) return DES_ERR_ARG;
+    Clock c;
+    int rc = read_clock(g, c);
+    if (rc) return rc;
+    r->steps = c.steps;
+    r->time = c.time;
+    r->dt = c.dt;
+    r->status = c.status;
+    r->ql_fallbacks = (long long)c.ql;
+    r->eigen_solves = (long long)c.eig;
+    return DES_OK;
+}
+
+int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)
+{
+    if (!g || nsteps < 0) return DES_ERR_ARG;
+    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (!g->primed) {
+        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
+        DES_LAUNCH();
+        g->primed = true;
+    }
+    if (!g->graph) {
+        int rc = capture_step_graph(g);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < nsteps; ++i) DES_CUDA(cudaGraphLaunch(g->graph, g->stream));
+    if (!report) return DES_OK;
+    int rc = des_gpu_report(g, report);
+    if (rc) return rc;
+    if (report->status & DES_STATUS_DT_NONPOSITIVE) return DES_ERR_DT;
+    return DES_OK;
+}
+
+int des_gpu_time_steps(des_gpu *g, int nsteps, double *ms)
+{
+    if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
+    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (!g->primed) {
+        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
+        DES_LAUNCH();
+        g->primed = true;
+    }
+    if (!g->graph) {
+        int rc = capture_step_graph(g);
+        if (rc) return rc;
+    }
+    cudaEvent_t a, b;
+    DES_CUDA(cudaEventCreate(&a));
+    DES_CUDA(cudaEventCreate(&b));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    DES_CUDA(cudaEventRecord(a, g->stream));
+    for (int i = 0; i < nsteps; ++i) DES_CUDA(cudaGraphLaunch(g->graph, g->stream));
+    DES_CUDA(cudaEventRecord(b, g->stream));
+    DES_CUDA(cudaEventSynchronize(b));
+    float f = 0;
+    DES_CUDA(cudaEventElapsedTime(&f, a, b));
+    *ms = f;
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return DES_OK;
+}
+
+int des_gpu_profile_steps(des_gpu *g, int nsteps, double ms[6])
+{
+    if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
+    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (!g->primed) {
+        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
+        DES_LAUNCH();
+        g->primed = true;
+    }
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; ++i) DES_CUDA(cudaEventCreate(&ev[i]));
+    for (int k = 0; k < 6; ++k) ms[k] = 0;
+    const Dev &d = g->d;
+    const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    for (int s = 0; s < nsteps; ++s) {
+        cudaEventRecord(ev[0], g->stream);
+        k_fn_a<<<nb, kNodeBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[1], g->stream);
+        k_fe_b<<<eb, kElemBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[2], g->stream);
+        k_sg_gather<<<nb, kNodeBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[3], g->stream);
+        k_fe_c<<<eb, kElemBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[4], g->stream);
+        k_fn_c<<<nb, kNodeBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[5], g->stream);
+        k_fe_a<<<eb, kElemBlock, 0, g->stream>>>(d);
+        cudaEventRecord(ev[6], g->stream);
+        DES_LAUNCH();
+        DES_CUDA(cudaEventSynchronize(ev[6]));
+        for (int k = 0; k < 6; ++k) {
+            float f = 0;
+            cudaEventElapsedTime(&f, ev[k], ev[k + 1]);
+            ms[k] += f;
+        }
+    }
+    for (int i = 0; i < 7; ++i) cudaEventDestroy(ev[i]);
+    return DES_OK;
+}
+
+int des_host_register(void *ptr, long long bytes)
+{
+    if (!ptr || bytes <= 0) return DES_ERR_ARG;
+    return cuda_rc(cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault));
+}
+int des_host_unregister(void *ptr)
+{
+    if (!ptr) return DES_ERR_ARG;
+    return cuda_rc(cudaHostUnregister(ptr));
+}
+void des_abi_sizes(long long out[5])
+{
+    out[0] = sizeof(des_params);
+    out[1] = sizeof(des_mesh_view);
+    out[2] = sizeof(des_state_view);
+    out[3] = sizeof(des_topology);
+    out[4] = sizeof(des_step_report);
+}
+
+int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
+                      des_step_report *report)
+{
+    int rc = des_gpu_upload(g, host, mask);
+    if (rc) return rc;
+    rc = des_gpu_step(g, nsteps, report);
+    if (rc) return rc;
+    return des_gpu_download(g, host, mask);
+}
+
+#define ELEM_GRID(g) blocks((g)->nelem, kElemBlock), kElemBlock, 0, (g)->stream
+#define NODE_GRID(g) blocks((g)->nnode, kNodeBlock), kNodeBlock, 0, (g)->stream
+
+int des_gpu_update_temperature(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_temp_elem<<<ELEM_GRID(g)>>>(g->d);
+    k_temp_node<<<NODE_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_update_strain_rate(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_srate<<<ELEM_GRID(g)>>>(g->d, g->d.srate);
+    return finish(g);
+}
+int des_gpu_compute_dvoldt(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_dvoldt_elem<<<ELEM_GRID(g)>>>(g->d);
+    k_sg_gather<<<NODE_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_compute_edvoldt(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_edvoldt<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_update_stress(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_stress<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_NMD_stress(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_dp_elem<<<ELEM_GRID(g)>>>(g->d);
+    k_sg_gather<<<NODE_GRID(g)>>>(g->d);
+    k_nmd_apply<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_update_force(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    k_force_elem<<<ELEM_GRID(g)>>>(g->d);
+    k_force_node<<<NODE_GRID(g)>>>(g->d, g->hK.is_qs);
+    return finish(g);
+}
+int des_gpu_update_velocity(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_velocity<<<NODE_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_apply_vbcs(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_vbcs<<<NODE_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_update_coordinate(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_coord<<<NODE_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_compute_volume(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_volume<<<ELEM_GRID(g)>>>(g->d, 0);
+    return finish(g);
+}
+int des_gpu_compute_mass(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_mass_elem<<<ELEM_GRID(g)>>>(g->d, g->d.T);
+    k_mass_node<<<NODE_GRID(g)>>>(g->d);
+    k_clock_mass_valid<<<1, 32, 0, g->stream>>>(g->dclk, 1);
+    return finish(g);
+}
+int des_gpu_compute_shape_fn(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_shape<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_update_mesh(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_coord<<<NODE_GRID(g)>>>(g->d);
+    k_volume<<<ELEM_GRID(g)>>>(g->d, 1);
+    k_mass_elem<<<ELEM_GRID(g)>>>(g->d, g->d.T);
+    k_mass_node<<<NODE_GRID(g)>>>(g->d);
+    k_clock_mass_valid<<<1, 32, 0, g->stream>>>(g->dclk, 1);
+    k_shape<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_rotate_stress(des_gpu *g)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    k_rotate<<<ELEM_GRID(g)>>>(g->d);
+    return finish(g);
+}
+int des_gpu_compute_dt(des_gpu *g, double *dt_out)
+{
+    int rc = begin_fn(g);
+    if (rc) return rc;
+    if (g->P.fixed_dt != 0) {
+        k_clock_dt<<<1, 32, 0, g->stream>>>(g->dclk, g->P.fixed_dt);
+    } else {
+        k_dt<<<ELEM_GRID(g)>>>(g->d);
+    }
+    if ((rc = finish(g))) return rc;
+    Clock c;
+    if ((rc = read_clock(g, c))) return rc;
+    if (dt_out) *dt_out = c.dt;
+    return (c.dt > 0) ? DES_OK : DES_ERR_DT;
+}
+
+int des_gpu_init_fields(des_gpu *g)
+{
+    if (!g) return DES_ERR_ARG;
+    const size_t N = g->nnode, E = g->nelem;
+    Dev &d = g->d;
+    g->primed = false;
+    cudaStream_t s = g->stream;
+    DES_CUDA(cudaMemsetAsync(d.vx, 0, sizeof(double) * 3 * N, s));
+    DES_CUDA(cudaMemsetAsync(d.fx, 0, sizeof(double) * 3 * N, s));
+    DES_CUDA(cudaMemsetAsync(d.stress, 0, sizeof(double) * 6 * E, s));
+    DES_CUDA(cudaMemsetAsync(d.strain, 0, sizeof(double) * 6 * E, s));
+    DES_CUDA(cudaMemsetAsync(d.srate, 0, sizeof(double) * 6 * E, s));
+    DES_CUDA(cudaMemcpyAsync(d.x0, d.x, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+    k_volume<<<ELEM_GRID(g)>>>(d, 0);
+    DES_CUDA(cudaMemcpyAsync(d.vol_old, d.vol, sizeof(double) * E, cudaMemcpyDeviceToDevice, s));
+    k_mass_elem<<<ELEM_GRID(g)>>>(d, nullptr);
+    k_mass_node<<<NODE_GRID(g)>>>(d);
+    k_clock_set<<<1, 32, 0, s>>>(g->dclk, 0.0, 0.0, 0, 1);
+    k_shape<<<ELEM_GRID(g)>>>(d);
+    k_vbcs<<<NODE_GRID(g)>>>(d);
+    if (g->P.gravity != 0) {
+        k_init_stress<<<ELEM_GRID(g)>>>(d);
+        g->P.compensation_pressure = g->P.rho0.v[0] * g->P.gravity * g->P.zlength;
+    } else {
+        g->P.compensation_pressure = 0;
+    }
+    g->hK.compensation_pressure = g->P.compensation_pressure;
+    DES_CUDA(cudaMemcpyAsync(&g->dK->compensation_pressure, &g->hK.compensation_pressure,
+                             sizeof(double), cudaMemcpyHostToDevice, s));
+    int rc = finish(g);
+    if (rc) return rc;
+    double dt;
+    return des_gpu_compute_dt(g, &dt);
+}
+
+}  // extern "C"

@@ -1,0 +1,1040 @@
+// Kernels of the FP64 step.  Two families share the device arithmetic of
+// des_device.cuh:
+//  * one kernel (or elem + node pair) per reference function, operating on
+//    the reference's fields, used by the per-function entry points;
+//  * six fused passes per time step (node / element alternating), captured
+//    into one CUDA graph:
+//      N-A  nodal masses (if stale), dvoldt gather, tdot gather + T update
+//      E-B  edvoldt, update_stress, dp * volume
+//      N-B  dp_nd gather
+//      E-C  NMD correction, element force vectors
+//      N-C  force gather, damping, velocity, velocity BCs, coordinates
+//      E-A  volume, shape functions, mass contributions, rotate_stress,
+//           next strain rate, dvoldt and conduction contributions, dt minimum
+// Every nodal sum runs over the node's support list in ascending element
+// order, as the reference's node loops do, so sums are bit-identical and
+// no atomics are needed.
+#pragma once
+
+#include "des_device.cuh"
+
+namespace des {
+
+struct Consts {
+    MatTable M;
+    double gravity, damping_factor, surface_temperature, dt_fraction, fixed_dt;
+    double inertial_scaling, max_vbc_val, therm_diff_max, zlength, rho0_0;
+    double compensation_pressure;
+    int damping_option, is_qs, thermal, rheol;
+    int vbc_types[10];
+    double vbc_values[10];
+    double bnormals[10][3];
+    double edge[10][10][3];
+};
+
+struct Clock {
+    double dt, time;
+    int steps, mass_valid;
+    unsigned long long minl, dtdiff;   // order_bits of running minima
+    unsigned blocks_done, status;
+    unsigned long long ql, eig;
+};
+
+struct Dev {
+    int nnode, nelem;
+    const int4 *conn;
+    const int *sup_off;
+    const unsigned *sup_ent;     // (element << 2) | local slot
+    const unsigned *bcflag;
+    const unsigned char *mix;
+    double *x, *y, *z, *vx, *vy, *vz, *fx, *fy, *fz, *x0, *y0, *z0;
+    double *T, *mass, *tmass, *vol_n, *ntmp;
+    double *vol, *vol_old, *edvoldt, *pls, *dpls, *dp, *tmp_sg;
+    double *stress, *strain, *srate, *srate_next;   // [6][E]
+    double *shp;                                     // [12][E] dx0..3 dy0..3 dz0..3
+    double *tmp;                                     // [12][E]
+    double *c_mass, *c_tmass, *c_trdv;               // fused-pass contributions
+    const Consts *K;
+    Clock *clk;
+};
+
+__device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
+
+__device__ __forceinline__ void load_xyz4(const Dev &d, int4 c, double X[4][3])
+{
+    const int n[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        X[i][0] = __ldg(d.x + n[i]);
+        X[i][1] = __ldg(d.y + n[i]);
+        X[i][2] = __ldg(d.z + n[i]);
+    }
+}
+__device__ __forceinline__ void load_vel4(const Dev &d, int4 c, double V[4][3])
+{
+    const int n[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        V[i][0] = __ldg(d.vx + n[i]);
+        V[i][1] = __ldg(d.vy + n[i]);
+        V[i][2] = __ldg(d.vz + n[i]);
+    }
+}
+__device__ __forceinline__ void load_nodal4(const double *a, int4 c, double out[4])
+{
+    out[0] = __ldg(a + c.x);
+    out[1] = __ldg(a + c.y);
+    out[2] = __ldg(a + c.z);
+    out[3] = __ldg(a + c.w);
+}
+__device__ __forceinline__ void load_shp(const Dev &d, int e, double dx[4], double dy[4],
+                                         double dz[4])
+{
+    const size_t E = d.nelem;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        dx[i] = d.shp[(0 + i) * E + e];
+        dy[i] = d.shp[(4 + i) * E + e];
+        dz[i] = d.shp[(8 + i) * E + e];
+    }
+}
+__device__ __forceinline__ void store_shp(const Dev &d, int e, const double dx[4], const double dy[4],
+                                          const double dz[4])
+{
+    const size_t E = d.nelem;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        d.shp[(0 + i) * E + e] = dx[i];
+        d.shp[(4 + i) * E + e] = dy[i];
+        d.shp[(8 + i) * E + e] = dz[i];
+    }
+}
+__device__ __forceinline__ void load6(const double *a, size_t E, int e, double s[6])
+{
+#pragma unroll
+    for (int i = 0; i < 6; ++i) s[i] = a[i * E + e];
+}
+__device__ __forceinline__ void store6(double *a, size_t E, int e, const double s[6])
+{
+#pragma unroll
+    for (int i = 0; i < 6; ++i) a[i * E + e] = s[i];
+}
+
+// ---- shared per-element / per-node bodies ---------------------------------
+
+// rheology.cxx:525-646 for one element; returns eigen flags (bit0 solved,
+// bit1 QL, bit2 QL failed)
+__device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double edv, double dt,
+                                           double s[6], double es[6], double edot[6], double &pls,
+                                           double &dpls, double &dpress)
+{
+    const Consts &K = *d.K;
+    const MatTable &M = K.M;
+    const Mix &x = M.mix[d.mix[e]];
+    double old_s = tr3(s);
+    {
+        double div = tr3(edot);
+        for (int i = 0; i < 3; ++i) edot[i] += (edv - div) / 3;
+    }
+    for (int i = 0; i < 6; ++i) es[i] += edot[i] * dt;
+    double de[6];
+    for (int i = 0; i < 6; ++i) de[i] = edot[i] * dt;
+    int flags = 0;
+    switch (K.rheol) {
+    case 1:   // elastic
+        elastic(x.bulkm, x.shearm, de, s);
+        break;
+    case 2: { // viscous
+        double Tn[4];
+        load_nodal4(d.T, c, Tn);
+        double viscosity = mat_visc(M, x, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]), edot);
+        viscous(x.bulkm, viscosity, tr3(es), edot, s);
+    } break;
+    case 3: { // maxwell
+        double Tn[4];
+        load_nodal4(d.T, c, Tn);
+        double viscosity = mat_visc(M, x, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]), edot);
+        double dv = d.vol[e] / d.vol_old[e] - 1;
+        maxwell(x.bulkm, x.shearm, viscosity, dt, dv, de, s);
+    } break;
+    case 5: { // elasto-plastic
+        double depls = 0;
+        double amc, anphi, anpsi, hardn, ten_max;
+        plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
+        flags = elasto_plastic(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, s);
+        pls += depls;
+        dpls = depls;
+    } break;
+    case 7: { // elasto-visco-plastic
+        double depls = 0;
+        double Tn[4];
+        load_nodal4(d.T, c, Tn);
+        double viscosity = mat_visc(M, x, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]), edot);
+        double dv = d.vol[e] / d.vol_old[e] - 1;
+        double sv[6];
+        for (int i = 0; i < 6; ++i) sv[i] = s[i];
+        maxwell(x.bulkm, x.shearm, viscosity, dt, dv, de, sv);
+        double svII = second_invariant2(sv);
+        double amc, anphi, anpsi, hardn, ten_max;
+        plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
+        double sp[6];
+        for (int i = 0; i < 6; ++i) sp[i] = s[i];
+        flags = elasto_plastic(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp);
+        double spII = second_invariant2(sp);
+        if (svII < spII) {
+            for (int i = 0; i < 6; ++i) s[i] = sv[i];
+        } else {
+            for (int i = 0; i < 6; ++i) s[i] = sp[i];
+            pls += depls;
+            dpls = depls;
+        }
+    } break;
+    }
+    dpress = tr3(s) - old_s;
+    return flags;
+}
+
+__device__ __forceinline__ void count_eigen(const Dev &d, int flags)
+{
+    // warp-aggregated counters of eigen-solves and QL fallbacks
+    unsigned solved = __ballot_sync(0xffffffffu, flags & 1);
+    unsigned ql = __ballot_sync(0xffffffffu, flags & 2);
+    unsigned bad = __ballot_sync(0xffffffffu, flags & 4);
+    if ((threadIdx.x & 31) == 0) {
+        if (solved) atomicAdd(&d.clk->eig, (unsigned long long)__popc(solved));
+        if (ql) atomicAdd(&d.clk->ql, (unsigned long long)__popc(ql));
+        if (bad) atomicOr(&d.clk->status, 0x8u);
+    }
+}
+
+// fields.cxx:264-297 for one component
+__device__ __forceinline__ double damp(const Consts &K, double f, double v)
+{
+    switch (K.damping_option) {
+    case 1:
+        if (fabs(v) > 1e-13) f -= K.damping_factor * copysign(f, v);
+        break;
+    case 2:
+        f -= K.damping_factor * f;
+        break;
+    case 3:
+        if ((f < 0) == (v < 0))
+            f -= K.damping_factor * f;
+        else
+            f += (1 - K.damping_factor) * f;
+        break;
+    default:
+        break;
+    }
+    return f;
+}
+
+// bc.cxx:201-496 for one node
+__device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double v[3])
+{
+    if (!(flag & kBoundAny)) return;
+    const int vx0 = K.vbc_types[0], vx1 = K.vbc_types[1], vy0 = K.vbc_types[2],
+              vy1 = K.vbc_types[3], vz0 = K.vbc_types[4], vz1 = K.vbc_types[5];
+    const double ux0 = K.vbc_values[0], ux1 = K.vbc_values[1], uy0 = K.vbc_values[2],
+                 uy1 = K.vbc_values[3], uz0 = K.vbc_values[4], uz1 = K.vbc_values[5];
+    if (flag & kBoundX0) {
+        switch (vx0) {
+        case 1: v[0] = ux0; break;
+        case 2: v[1] = 0; v[2] = 0; break;
+        case 3: v[0] = ux0; v[1] = 0; v[2] = 0; break;
+        case 4: v[1] = ux0; v[2] = 0; break;
+        case 5: v[0] = 0; v[1] = ux0; v[2] = 0; break;
+        case 7: v[0] = ux0; v[1] = 0; break;
+        }
+    }
+    if (flag & kBoundX1) {
+        switch (vx1) {
+        case 1: v[0] = ux1; break;
+        case 2: v[1] = 0; v[2] = 0; break;
+        case 3: v[0] = ux1; v[1] = 0; v[2] = 0; break;
+        case 4: v[1] = ux1; v[2] = 0; break;
+        case 5: v[0] = 0; v[1] = ux1; v[2] = 0; break;
+        case 7: v[0] = ux1; v[1] = 0; break;
+        }
+    }
+    if (flag & kBoundY0) {
+        switch (vy0) {
+        case 1: v[1] = uy0; break;
+        case 2: v[0] = 0; v[2] = 0; break;
+        case 3: v[0] = 0; v[1] = uy0; v[2] = 0; break;
+        case 4: v[0] = uy0; v[2] = 0; break;
+        case 5: v[0] = uy0; v[1] = 0; v[2] = 0; break;
+        case 7: v[0] = 0; v[1] = uy0; break;
+        }
+    }
+    if (flag & kBoundY1) {
+        switch (vy1) {
+        case 1: v[1] = uy1; break;
+        case 2: v[0] = 0; v[2] = 0; break;
+        case 3: v[0] = uy1; v[1] = 0; v[2] = 0; break;
+        case 4: v[0] = uy1; v[2] = 0; break;
+        case 5: v[0] = uy1; v[1] = 0; v[2] = 0; break;
+        case 7: v[0] = 0; v[1] = uy1; break;
+        }
+    }
+    if (flag & 0x3c0u) {
+        for (int ib = 6; ib <= 9; ib++) {
+            if (!(flag & (1u << ib))) continue;
+            const double *n = K.bnormals[ib];
+            double fac = 0;
+            switch (K.vbc_types[ib]) {
+            case 1:
+                if (flag == (1u << ib)) {
+                    double vn = 0;
+                    for (int dd = 0; dd < 3; dd++) vn += v[dd] * n[dd];
+                    for (int dd = 0; dd < 3; dd++) v[dd] += (K.vbc_values[ib] - vn) * n[dd];
+                } else {
+                    for (int ic = 0; ic < ib; ic++) {
+                        if (!(flag & (1u << ic))) continue;
+                        if (K.vbc_types[ic] == 0) {
+                            double vn = 0;
+                            for (int dd = 0; dd < 3; dd++) vn += v[dd] * n[dd];
+                            for (int dd = 0; dd < 3; dd++) v[dd] += (K.vbc_values[ib] - vn) * n[dd];
+                        } else if (K.vbc_types[ic] == 1) {
+                            const double *edge = K.edge[ic][ib];
+                            double ve = 0;
+                            for (int dd = 0; dd < 3; dd++) ve += v[dd] * edge[dd];
+                            for (int dd = 0; dd < 3; dd++) v[dd] = ve * edge[dd];
+                        }
+                    }
+                }
+                break;
+            case 3:
+                for (int dd = 0; dd < 3; dd++) v[dd] = K.vbc_values[ib] * n[dd];
+                break;
+            case 11:
+                fac = 1 / sqrt(1 - n[2] * n[2]);
+                if (flag == (1u << ib)) {
+                    double vn = 0;
+                    for (int dd = 0; dd < 2; dd++) vn += v[dd] * n[dd];
+                    for (int dd = 0; dd < 2; dd++) v[dd] += (K.vbc_values[ib] * fac - vn) * n[dd];
+                } else {
+                    for (int ic = 0; ic < ib; ic++) {
+                        if (!(flag & (1u << ic))) continue;
+                        if (K.vbc_types[ic] == 0) {
+                            double vn = 0;
+                            for (int dd = 0; dd < 2; dd++) vn += v[dd] * n[dd];
+                            for (int dd = 0; dd < 2; dd++)
+                                v[dd] += (K.vbc_values[ib] * fac - vn) * n[dd];
+                        } else if (K.vbc_types[ic] == 1) {
+                            const double *edge = K.edge[ic][ib];
+                            double ve = 0;
+                            for (int dd = 0; dd < 3; dd++) ve += v[dd] * edge[dd];
+                            for (int dd = 0; dd < 3; dd++) v[dd] = ve * edge[dd];
+                        }
+                    }
+                }
+                break;
+            case 13:
+                fac = 1 / sqrt(1 - n[2] * n[2]);
+                for (int dd = 0; dd < 2; dd++) v[dd] = K.vbc_values[ib] * fac * n[dd];
+                v[2] = 0;
+                break;
+            }
+        }
+    }
+    if (vz0 == 0 && vz1 == 0) return;
+    if (flag & kBoundZ0) {
+        switch (vz0) {
+        case 1: v[2] = uz0; break;
+        case 2: v[0] = 0; v[1] = 0; break;
+        case 3: v[0] = 0; v[1] = 0; v[2] = uz0; break;
+        }
+    }
+    if (flag & kBoundZ1) {
+        switch (vz1) {
+        case 1: v[2] = uz1; break;
+        case 2: v[0] = 0; v[1] = 0; break;
+        case 3: v[0] = 0; v[1] = 0; v[2] = uz1; break;
+        }
+    }
+}
+
+// geometry.cxx:271-309 for one element: minh and its dt_diffusion candidate
+__device__ __forceinline__ double min_height(const double X[4][3], double vol)
+{
+    double maxa = smax(smax(tri_area(X[0], X[1], X[2]), tri_area(X[0], X[1], X[3])),
+                       smax(tri_area(X[2], X[3], X[0]), tri_area(X[2], X[3], X[1])));
+    return 3 * vol / maxa;
+}
+
+// block-level minimum of two values + the last block turns the global minima
+// into dt (geometry.cxx:311-325).  No thread waits on another block.
+__device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff, bool active)
+{
+    __shared__ unsigned long long s_min[32], s_dif[32];
+    __shared__ bool s_last;
+    unsigned long long a = active ? order_bits(minh) : ~0ULL;
+    unsigned long long b = active ? order_bits(dtdiff) : ~0ULL;
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long a2 = __shfl_down_sync(0xffffffffu, a, o);
+        unsigned long long b2 = __shfl_down_sync(0xffffffffu, b, o);
+        a = a2 < a ? a2 : a;
+        b = b2 < b ? b2 : b;
+    }
+    int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s_min[warp] = a;
+        s_dif[warp] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long ma = ~0ULL, mb = ~0ULL;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) {
+            ma = s_min[w] < ma ? s_min[w] : ma;
+            mb = s_dif[w] < mb ? s_dif[w] : mb;
+        }
+        if (ma != ~0ULL) atomicMin(&d.clk->minl, ma);
+        if (mb != ~0ULL) atomicMin(&d.clk->dtdiff, mb);
+        __threadfence();
+        unsigned done = atomicAdd(&d.clk->blocks_done, 1u);
+        s_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        const Consts &K = *d.K;
+        unsigned long long bl = atomicAdd(&d.clk->minl, 0ULL);
+        unsigned long long bd = atomicAdd(&d.clk->dtdiff, 0ULL);
+        double minl = from_order_bits(bl);
+        double dt_diffusion = K.thermal ? from_order_bits(bd) : 1.7976931348623157e308;
+        double dt_maxwell = 1.7976931348623157e308;
+        for (int i = 0; i < K.M.nmix; ++i) dt_maxwell = smin(dt_maxwell, K.M.mix[i].dt_maxwell);
+        double dt_advection = 0.5 * minl / K.max_vbc_val;
+        double dt_elastic;
+        if (K.is_qs) {
+            dt_elastic = 0.5 * minl / (K.max_vbc_val * K.inertial_scaling);
+        } else {
+            int4 c0 = d.conn[0];
+            double Tn[4];
+            load_nodal4(d.T, c0, Tn);
+            const Mix &x0 = K.M.mix[d.mix[0]];
+            double rho0 = mat_rho(K.M, x0, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]));
+            dt_elastic = 0.5 * minl / sqrt(x0.bulkm / rho0);
+        }
+        double dt = smin(smin(dt_elastic, dt_maxwell), smin(dt_advection, dt_diffusion)) * K.dt_fraction;
+        d.clk->dt = dt;
+        if (!(dt > 0)) atomicOr(&d.clk->status, 0x1u);
+        d.clk->minl = ~0ULL;
+        d.clk->dtdiff = ~0ULL;
+        d.clk->blocks_done = 0;
+    }
+}
+
+// ===========================================================================
+// per-function kernels
+// ===========================================================================
+
+// fields.cxx:119-144
+__global__ void k_temp_elem(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    int4 c = d.conn[e];
+    double dx[4], dy[4], dz[4], Tn[4], tr[4];
+    load_shp(d, e, dx, dy, dz);
+    load_nodal4(d.T, c, Tn);
+    double kv = d.K->M.mix[d.mix[e]].k * d.vol[e];
+    conduction(dx, dy, dz, Tn, kv, tr);
+    for (int i = 0; i < 4; ++i) d.tmp[i * E + e] = tr[i];
+}
+
+// fields.cxx:149-168
+__global__ void k_temp_node(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    const size_t E = d.nelem;
+    double tdot = 0;
+    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) {
+        unsigned p = __ldg(d.sup_ent + q);
+        tdot += d.tmp[(p & 3u) * E + (p >> 2)];
+    }
+    d.ntmp[n] = tdot;
+    const Consts &K = *d.K;
+    if (d.bcflag[n] & kBoundZ1)
+        d.T[n] = K.surface_temperature;
+    else
+        d.T[n] -= tdot * d.clk->dt / d.tmass[n];
+}
+
+// fields.cxx:184-243; out = srate or srate_next
+__global__ void k_srate(Dev d, double *out)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    double V[4][3], dx[4], dy[4], dz[4], s[6];
+    load_vel4(d, d.conn[e], V);
+    load_shp(d, e, dx, dy, dz);
+    strain_rate(V, dx, dy, dz, s);
+    store6(out, d.nelem, e, s);
+}
+
+// geometry.cxx:128-134 (src = srate) and 200-204 (dp)
+__global__ void k_dvoldt_elem(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    double dj = d.srate[e] + d.srate[E + e] + d.srate[2 * E + e];
+    d.tmp_sg[e] = dj * d.vol[e];
+}
+__global__ void k_dp_elem(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    d.tmp_sg[e] = d.dp[e] * d.vol[e];
+}
+
+// geometry.cxx:138-143 and 208-213: ntmp[n] = sum(tmp_sg) / volume_n
+__global__ void k_sg_gather(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    double s = 0.;
+    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) s += d.tmp_sg[__ldg(d.sup_ent + q) >> 2];
+    s /= d.vol_n[n];
+    d.ntmp[n] = s;
+}
+
+// geometry.cxx:166-174
+__global__ void k_edvoldt(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    double a[4];
+    load_nodal4(d.ntmp, d.conn[e], a);
+    double dj = 0;
+    for (int i = 0; i < 4; ++i) dj += a[i];
+    d.edvoldt[e] = dj / 4;
+}
+
+// rheology.cxx:525-650
+__global__ void k_stress(Dev d)
+{
+    int e = gtid();
+    bool live = e < d.nelem;
+    int flags = 0;
+    if (live) {
+        const size_t E = d.nelem;
+        double s[6], es[6], edot[6];
+        load6(d.stress, E, e, s);
+        load6(d.strain, E, e, es);
+        load6(d.srate, E, e, edot);
+        double pls = d.pls[e], dpls = d.dpls[e], dpress;
+        flags = stress_body(d, e, d.conn[e], d.edvoldt[e], d.clk->dt, s, es, edot, pls, dpls, dpress);
+        store6(d.stress, E, e, s);
+        store6(d.strain, E, e, es);
+        store6(d.srate, E, e, edot);
+        d.pls[e] = pls;
+        d.dpls[e] = dpls;
+        d.dp[e] = dpress;
+    }
+    count_eigen(d, flags);
+}
+
+// geometry.cxx:221-250
+__global__ void k_nmd_apply(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    double a[4];
+    load_nodal4(d.ntmp, d.conn[e], a);
+    double dpe = 0;
+    for (int i = 0; i < 4; ++i) dpe += a[i];
+    double dp_el = dpe / 4;
+    double ddp = (-d.dp[e] + dp_el) / 3;
+    for (int i = 0; i < 3; ++i) d.stress[i * E + e] += ddp;
+}
+
+// fields.cxx:321-346: element force vectors into tmp[12][E]
+__device__ __forceinline__ void force_elem_body(const Dev &d, int e, int4 c, const double s[6])
+{
+    const size_t E = d.nelem;
+    const Consts &K = *d.K;
+    double dx[4], dy[4], dz[4];
+    load_shp(d, e, dx, dy, dz);
+    double vol = d.vol[e];
+    double buoy = 0;
+    if (K.gravity != 0) {
+        double Tn[4];
+        load_nodal4(d.T, c, Tn);
+        buoy = mat_rho(K.M, K.M.mix[d.mix[e]], elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3])) * K.gravity / 4;
+    }
+    for (int i = 0; i < 4; ++i) {
+        d.tmp[(i)*E + e] = (s[0] * dx[i] + s[3] * dy[i] + s[4] * dz[i]) * vol;
+        d.tmp[(i + 4) * E + e] = (s[3] * dx[i] + s[1] * dy[i] + s[5] * dz[i]) * vol;
+        d.tmp[(i + 8) * E + e] = (s[4] * dx[i] + s[5] * dy[i] + s[2] * dz[i] + buoy) * vol;
+    }
+}
+__global__ void k_force_elem(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    double s[6];
+    load6(d.stress, d.nelem, e, s);
+    force_elem_body(d, e, d.conn[e], s);
+}
+
+// fields.cxx:351-365 + apply_damping (fields.cxx:250-309)
+__device__ __forceinline__ void force_gather(const Dev &d, int n, double f[3])
+{
+    const size_t E = d.nelem;
+    f[0] = f[1] = f[2] = 0;
+    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) {
+        unsigned p = __ldg(d.sup_ent + q);
+        size_t e = p >> 2, i = p & 3u;
+        f[0] -= d.tmp[(i)*E + e];
+        f[1] -= d.tmp[(i + 4) * E + e];
+        f[2] -= d.tmp[(i + 8) * E + e];
+    }
+}
+__global__ void k_force_node(Dev d, int damping)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    double f[3];
+    force_gather(d, n, f);
+    if (damping) {
+        const Consts &K = *d.K;
+        f[0] = damp(K, f[0], d.vx[n]);
+        f[1] = damp(K, f[1], d.vy[n]);
+        f[2] = damp(K, f[2], d.vz[n]);
+    }
+    d.fx[n] = f[0];
+    d.fy[n] = f[1];
+    d.fz[n] = f[2];
+}
+
+// fields.cxx:386-389
+__global__ void k_velocity(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    double dt = d.clk->dt, m = d.mass[n];
+    d.vx[n] += dt * d.fx[n] / m;
+    d.vy[n] += dt * d.fy[n] / m;
+    d.vz[n] += dt * d.fz[n] / m;
+}
+
+__global__ void k_vbcs(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    unsigned flag = d.bcflag[n];
+    if (!(flag & kBoundAny)) return;
+    double v[3] = {d.vx[n], d.vy[n], d.vz[n]};
+    vbc_node(*d.K, flag, v);
+    d.vx[n] = v[0];
+    d.vy[n] = v[1];
+    d.vz[n] = v[2];
+}
+
+// fields.cxx:406-408
+__global__ void k_coord(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    double dt = d.clk->dt;
+    d.x[n] += d.vx[n] * dt;
+    d.y[n] += d.vy[n] * dt;
+    d.z[n] += d.vz[n] * dt;
+}
+
+// geometry.cxx:94-110; save_old copies volume into volume_old first
+__global__ void k_volume(Dev d, int save_old)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    double X[4][3];
+    load_xyz4(d, d.conn[e], X);
+    double v = tet_volume(X[0], X[1], X[2], X[3]);
+    if (save_old) d.vol_old[e] = d.vol[e];
+    d.vol[e] = v;
+    if (!(v > 0)) atomicOr(&d.clk->status, 0x4u);
+}
+
+// geometry.cxx:354-365; Tsrc = NULL means T = 0 (the first compute_mass of init)
+__global__ void k_mass_elem(Dev d, const double *Tsrc)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    const Consts &K = *d.K;
+    const Mix &x = K.M.mix[d.mix[e]];
+    double Tn[4] = {0, 0, 0, 0};
+    if (Tsrc) load_nodal4(Tsrc, d.conn[e], Tn);
+    double rT = mat_rho(K.M, x, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]));
+    double vol = d.vol[e];
+    double rho = K.is_qs ? x.rho_qs : rT;
+    double m = rho * vol / 4;
+    double tm = rT * x.cp * vol / 4;
+    d.tmp[e] = vol;
+    d.tmp[E + e] = m;
+    if (K.thermal) d.tmp[2 * E + e] = tm;
+}
+
+// geometry.cxx:370-381 from tmp[0..2]
+__global__ void k_mass_node(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    const size_t E = d.nelem;
+    const bool thermal = d.K->thermal;
+    double vn = 0, m = 0, tm = 0;
+    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) {
+        size_t e = __ldg(d.sup_ent + q) >> 2;
+        vn += d.tmp[e];
+        m += d.tmp[E + e];
+        if (thermal) tm += d.tmp[2 * E + e];
+    }
+    d.vol_n[n] = vn;
+    d.mass[n] = m;
+    d.tmass[n] = tm;
+}
+
+// geometry.cxx:400-466
+__global__ void k_shape(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    double X[4][3], dx[4], dy[4], dz[4];
+    load_xyz4(d, d.conn[e], X);
+    shape_fn(X, d.vol[e], dx, dy, dz);
+    store_shp(d, e, dx, dy, dz);
+}
+
+// fields.cxx:478-529
+__global__ void k_rotate(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    double V[4][3], dx[4], dy[4], dz[4], w3, w4, w5, s[6];
+    load_vel4(d, d.conn[e], V);
+    load_shp(d, e, dx, dy, dz);
+    spin(V, dx, dy, dz, w3, w4, w5);
+    double dt = d.clk->dt;
+    load6(d.stress, E, e, s);
+    jaumann(s, dt, w3, w4, w5);
+    store6(d.stress, E, e, s);
+    load6(d.strain, E, e, s);
+    jaumann(s, dt, w3, w4, w5);
+    store6(d.strain, E, e, s);
+}
+
+// geometry.cxx:270-325
+__global__ void k_dt(Dev d)
+{
+    int e = gtid();
+    bool live = e < d.nelem;
+    double minh = 0, dtd = 0;
+    if (live) {
+        double X[4][3];
+        load_xyz4(d, d.conn[e], X);
+        minh = min_height(X, d.vol[e]);
+        dtd = 0.5 * minh * minh / d.K->therm_diff_max;
+    }
+    dt_reduce_and_finalize(d, minh, dtd, live);
+}
+
+// ic.cxx:100-131 (ref_pressure_option 0)
+__global__ void k_init_stress(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    const Consts &K = *d.K;
+    double ks = K.M.mix[d.mix[0]].bulkm;
+    double zn[4];
+    load_nodal4(d.z, d.conn[e], zn);
+    double zcenter = elem_mean4(zn[0], zn[1], zn[2], zn[3]);
+    double p = K.rho0_0 * K.gravity * (-zcenter);
+    for (int i = 0; i < 3; ++i) {
+        d.stress[i * E + e] = -p;
+        d.strain[i * E + e] = -p / ks / 3;
+    }
+}
+
+// ===========================================================================
+// fused passes
+// ===========================================================================
+
+// contributions for the next N-A pass from the current state: next strain
+// rate, tr(D) * volume, conduction vector
+__device__ __forceinline__ void next_step_contrib(const Dev &d, int e, int4 c, const double V[4][3],
+                                                  const double dx[4], const double dy[4],
+                                                  const double dz[4], double vol)
+{
+    const size_t E = d.nelem;
+    double D[6];
+    strain_rate(V, dx, dy, dz, D);
+    store6(d.srate_next, E, e, D);
+    d.c_trdv[e] = tr3(D) * vol;
+    if (d.K->thermal) {
+        double Tn[4], tr[4];
+        load_nodal4(d.T, c, Tn);
+        conduction(dx, dy, dz, Tn, d.K->M.mix[d.mix[e]].k * vol, tr);
+        for (int i = 0; i < 4; ++i) d.tmp[i * E + e] = tr[i];
+    }
+}
+
+__global__ void k_prime(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    int4 c = d.conn[e];
+    double V[4][3], dx[4], dy[4], dz[4];
+    load_vel4(d, c, V);
+    load_shp(d, e, dx, dy, dz);
+    next_step_contrib(d, e, c, V, dx, dy, dz, d.vol[e]);
+}
+
+// N-A: start of a step (dynearthsol.cxx:358-362, 365 node half)
+__global__ void k_fn_a(Dev d)
+{
+    int n = gtid();
+    const Consts &K = *d.K;
+    const double dt = d.clk->dt;
+    if (n == 0) {
+        d.clk->steps += 1;
+        d.clk->time += dt;
+    }
+    if (n >= d.nnode) return;
+    const size_t E = d.nelem;
+    const int q0 = d.sup_off[n], q1 = d.sup_off[n + 1];
+    double vn, tm;
+    if (d.clk->mass_valid) {
+        vn = d.vol_n[n];
+        tm = d.tmass[n];
+    } else {
+        double m = 0;
+        vn = 0;
+        tm = 0;
+        for (int q = q0; q < q1; ++q) {
+            size_t e = __ldg(d.sup_ent + q) >> 2;
+            vn += d.vol[e];
+            m += d.c_mass[e];
+            if (K.thermal) tm += d.c_tmass[e];
+        }
+        d.vol_n[n] = vn;
+        d.mass[n] = m;
+        d.tmass[n] = tm;
+    }
+    if (K.thermal) {
+        double tdot = 0;
+        for (int q = q0; q < q1; ++q) {
+            unsigned p = __ldg(d.sup_ent + q);
+            tdot += d.tmp[(p & 3u) * E + (p >> 2)];
+        }
+        if (d.bcflag[n] & kBoundZ1)
+            d.T[n] = K.surface_temperature;
+        else
+            d.T[n] -= tdot * dt / tm;
+    }
+    double dv = 0.;
+    for (int q = q0; q < q1; ++q) dv += d.c_trdv[__ldg(d.sup_ent + q) >> 2];
+    dv /= vn;
+    d.ntmp[n] = dv;
+}
+
+// E-B: edvoldt + update_stress + dp * volume
+__global__ void k_fe_b(Dev d)
+{
+    int e = gtid();
+    if (e == 0) d.clk->mass_valid = 1;
+    bool live = e < d.nelem;
+    int flags = 0;
+    if (live) {
+        const size_t E = d.nelem;
+        int4 c = d.conn[e];
+        double a[4];
+        load_nodal4(d.ntmp, c, a);
+        double dj = 0;
+        for (int i = 0; i < 4; ++i) dj += a[i];
+        double edv = dj / 4;
+        d.edvoldt[e] = edv;
+        double s[6], es[6], edot[6];
+        load6(d.stress, E, e, s);
+        load6(d.strain, E, e, es);
+        load6(d.srate_next, E, e, edot);
+        double pls = d.pls[e], dpls = d.dpls[e], dpress;
+        flags = stress_body(d, e, c, edv, d.clk->dt, s, es, edot, pls, dpls, dpress);
+        store6(d.stress, E, e, s);
+        store6(d.strain, E, e, es);
+        store6(d.srate, E, e, edot);
+        d.pls[e] = pls;
+        d.dpls[e] = dpls;
+        d.dp[e] = dpress;
+        d.tmp_sg[e] = dpress * d.vol[e];
+    }
+    count_eigen(d, flags);
+}
+
+// E-C: NMD correction + element force vectors
+__global__ void k_fe_c(Dev d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    const size_t E = d.nelem;
+    int4 c = d.conn[e];
+    double a[4];
+    load_nodal4(d.ntmp, c, a);
+    double dpe = 0;
+    for (int i = 0; i < 4; ++i) dpe += a[i];
+    double dp_el = dpe / 4;
+    double ddp = (-d.dp[e] + dp_el) / 3;
+    double s[6];
+    load6(d.stress, E, e, s);
+    for (int i = 0; i < 3; ++i) s[i] += ddp;
+    for (int i = 0; i < 3; ++i) d.stress[i * E + e] = s[i];
+    force_elem_body(d, e, c, s);
+}
+
+// N-C: force gather, damping, velocity, velocity BCs, coordinates
+__global__ void k_fn_c(Dev d)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    const Consts &K = *d.K;
+    const double dt = d.clk->dt;
+    double f[3];
+    force_gather(d, n, f);
+    double v[3] = {d.vx[n], d.vy[n], d.vz[n]};
+    if (K.is_qs) {
+        f[0] = damp(K, f[0], v[0]);
+        f[1] = damp(K, f[1], v[1]);
+        f[2] = damp(K, f[2], v[2]);
+    }
+    d.fx[n] = f[0];
+    d.fy[n] = f[1];
+    d.fz[n] = f[2];
+    double m = d.mass[n];
+    for (int j = 0; j < 3; ++j) v[j] += dt * f[j] / m;
+    vbc_node(K, d.bcflag[n], v);
+    d.vx[n] = v[0];
+    d.vy[n] = v[1];
+    d.vz[n] = v[2];
+    d.x[n] += v[0] * dt;
+    d.y[n] += v[1] * dt;
+    d.z[n] += v[2] * dt;
+}
+
+// E-A: update_mesh element half, rotate_stress, next-step contributions, dt
+__global__ void k_fe_a(Dev d)
+{
+    int e = gtid();
+    const Consts &K = *d.K;
+    const bool dt_step = (K.fixed_dt == 0) && (d.clk->steps % 10 == 0);
+    if (e == 0) d.clk->mass_valid = 0;
+    bool live = e < d.nelem;
+    double minh = 0, dtd = 0;
+    if (live) {
+        const size_t E = d.nelem;
+        int4 c = d.conn[e];
+        double X[4][3];
+        load_xyz4(d, c, X);
+        double vol = tet_volume(X[0], X[1], X[2], X[3]);
+        d.vol_old[e] = d.vol[e];
+        d.vol[e] = vol;
+        if (!(vol > 0)) atomicOr(&d.clk->status, 0x4u);
+        double dx[4], dy[4], dz[4];
+        shape_fn(X, vol, dx, dy, dz);
+        store_shp(d, e, dx, dy, dz);
+        const Mix &x = K.M.mix[d.mix[e]];
+        {
+            double Tn[4];
+            load_nodal4(d.T, c, Tn);
+            double rT = mat_rho(K.M, x, elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]));
+            double rho = K.is_qs ? x.rho_qs : rT;
+            d.c_mass[e] = rho * vol / 4;
+            if (K.thermal) d.c_tmass[e] = rT * x.cp * vol / 4;
+        }
+        double V[4][3];
+        load_vel4(d, c, V);
+        if (K.rheol & 1) {
+            double w3, w4, w5, s[6];
+            spin(V, dx, dy, dz, w3, w4, w5);
+            const double dt = d.clk->dt;
+            load6(d.stress, E, e, s);
+            jaumann(s, dt, w3, w4, w5);
+            store6(d.stress, E, e, s);
+            load6(d.strain, E, e, s);
+            jaumann(s, dt, w3, w4, w5);
+            store6(d.strain, E, e, s);
+        }
+        next_step_contrib(d, e, c, V, dx, dy, dz, vol);
+        if (dt_step) {
+            minh = min_height(X, vol);
+            dtd = 0.5 * minh * minh / K.therm_diff_max;
+        }
+    }
+    if (dt_step) dt_reduce_and_finalize(d, minh, dtd, live);
+}
+
+// nodal masses from the fused-pass contributions (used before a download)
+__global__ void k_mass_flush(Dev d)
+{
+    int n = gtid();
+    if (n == 0) d.clk->mass_valid = 1;
+    if (n >= d.nnode) return;
+    const bool thermal = d.K->thermal;
+    double vn = 0, m = 0, tm = 0;
+    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) {
+        size_t e = __ldg(d.sup_ent + q) >> 2;
+        vn += d.vol[e];
+        m += d.c_mass[e];
+        if (thermal) tm += d.c_tmass[e];
+    }
+    d.vol_n[n] = vn;
+    d.mass[n] = m;
+    d.tmass[n] = tm;
+}
+
+// ---- layout conversion ----------------------------------------------------
+// rows [row0, row0 + rows) of an AoS block with ncomp components <-> SoA
+__global__ void k_aos_to_soa(const double *src, double *dst, int ncomp, long long rows,
+                             long long row0, long long ld)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * ncomp) return;
+    long long r = i / ncomp;
+    int c = (int)(i - r * ncomp);
+    dst[c * ld + row0 + r] = src[i];
+}
+__global__ void k_soa_to_aos(const double *src, double *dst, int ncomp, long long rows,
+                             long long row0, long long ld)
+{
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * ncomp) return;
+    long long r = i / ncomp;
+    int c = (int)(i - r * ncomp);
+    dst[i] = src[c * ld + row0 + r];
+}
+
+__global__ void k_clock_set(Clock *clk, double time, double dt, int steps, int mass_valid)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        clk->time = time;
+        clk->dt = dt;
+        clk->steps = steps;
+        clk->mass_valid = mass_valid;
+    }
+}
+__global__ void k_clock_mass_valid(Clock *clk, int v)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) clk->mass_valid = v;
+}
+__global__ void k_clock_dt(Clock *clk, double dt)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) clk->dt = dt;
+}
+
+}  // namespace des

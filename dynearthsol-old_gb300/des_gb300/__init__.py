@@ -1,0 +1,218 @@
+"""Python host side of the GB300 DynEarthSol3D time-step library.
+
+The product is the C-ABI library libdes_gb300.so (include/des_gpu.h); this
+package loads it with ctypes and offers the reference's loop functions with
+their names (update_stress, update_force, ...) on a device-resident state.
+There is no CPU path: every compute call goes to the CUDA library, and loading
+fails loudly when the library is missing.
+"""
+import ctypes as C
+import os
+from pathlib import Path
+
+from . import abi
+from .abi import State, check
+from .build import LIB, build
+
+_lib = None
+
+FUNCTIONS = ["update_temperature", "update_strain_rate", "compute_dvoldt", "compute_edvoldt",
+             "update_stress", "NMD_stress", "update_force", "update_velocity", "apply_vbcs",
+             "update_coordinate", "compute_volume", "compute_mass", "compute_shape_fn",
+             "update_mesh", "rotate_stress"]
+
+
+def lib():
+    """Load libdes_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB.exists():
+        raise RuntimeError(f"{LIB} is missing: run des_gb300.build.build() first")
+    L = C.CDLL(str(LIB))
+    P = C.POINTER
+    L.des_box_sizes.argtypes = [P(abi.BoxSpec), P(C.c_int), P(C.c_int), P(C.c_int)]
+    L.des_box_fill.argtypes = [P(abi.BoxSpec), P(C.c_double), P(C.c_int), P(C.c_int), P(C.c_int)]
+    L.des_markers_layered.argtypes = [C.c_int, C.c_int, P(C.c_double), P(C.c_int), C.c_int,
+                                      C.c_double, C.c_int, P(C.c_int), P(C.c_double),
+                                      C.c_ulonglong, P(C.c_int)]
+    L.des_temperature_linear.argtypes = [C.c_int, P(C.c_double), C.c_double, C.c_double,
+                                         C.c_double, C.c_double, C.c_ulonglong, P(C.c_double)]
+    L.des_topology_build.argtypes = [P(abi.MeshView), P(P(abi.Topology))]
+    L.des_topology_free.argtypes = [P(abi.Topology)]
+    L.des_topology_free.restype = None
+    L.des_boundary_normals.argtypes = [P(abi.Topology), P(C.c_int), P(C.c_double), P(abi.Params)]
+    L.des_gpu_create.argtypes = [P(abi.MeshView), P(abi.Params), C.c_int, P(C.c_void_p)]
+    L.des_gpu_destroy.argtypes = [C.c_void_p]
+    L.des_gpu_set_params.argtypes = [C.c_void_p, P(abi.Params)]
+    L.des_gpu_upload.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
+    L.des_gpu_download.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
+    L.des_gpu_init_fields.argtypes = [C.c_void_p]
+    L.des_gpu_step.argtypes = [C.c_void_p, C.c_int, P(abi.StepReport)]
+    L.des_gpu_step_host.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint, C.c_int,
+                                    P(abi.StepReport)]
+    L.des_gpu_report.argtypes = [C.c_void_p, P(abi.StepReport)]
+    for f in FUNCTIONS:
+        getattr(L, "des_gpu_" + f).argtypes = [C.c_void_p]
+    L.des_gpu_compute_dt.argtypes = [C.c_void_p, P(C.c_double)]
+    L.des_gpu_error_string.argtypes = [C.c_int]
+    L.des_gpu_error_string.restype = C.c_char_p
+    L.des_gpu_device_bytes.argtypes = [C.c_void_p]
+    L.des_gpu_device_bytes.restype = C.c_longlong
+    L.des_gpu_kernels_per_step.argtypes = [C.c_void_p]
+    L.des_gpu_time_steps.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
+    L.des_gpu_profile_steps.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
+    L.des_host_register.argtypes = [C.c_void_p, C.c_longlong]
+    L.des_host_unregister.argtypes = [C.c_void_p]
+    L.des_abi_sizes.argtypes = [P(C.c_longlong)]
+    L.des_abi_sizes.restype = None
+    _lib = L
+    return L
+
+
+def _ck(rc, what):
+    if rc != abi.DES_OK:
+        msg = lib().des_gpu_error_string(rc).decode()
+        raise RuntimeError(f"{what}: error {rc} ({msg})")
+
+
+class Topology:
+    """bcflag, support lists, bnodes, bfacets as built by the library."""
+
+    def __init__(self, mesh):
+        import numpy as np
+        L = lib()
+        ptr = C.POINTER(abi.Topology)()
+        mv = mesh.view()
+        _ck(L.des_topology_build(C.byref(mv), C.byref(ptr)), "des_topology_build")
+        t = ptr.contents
+        N, E = mesh.nnode, mesh.nelem
+        self.bcflag = np.ctypeslib.as_array(t.bcflag, (N,)).copy()
+        self.support_offsets = np.ctypeslib.as_array(t.support_offsets, (N + 1,)).copy()
+        self.support_elems = np.ctypeslib.as_array(t.support_elems, (4 * E,)).copy()
+        self.support_slots = np.ctypeslib.as_array(t.support_slots, (4 * E,)).copy()
+        self.bnodes = [np.ctypeslib.as_array(t.bnodes[b], (t.bnodes_count[b],)).copy()
+                       if t.bnodes_count[b] else np.zeros(0, np.int32) for b in range(abi.DES_NBDRY)]
+        self.bfacets = [np.ctypeslib.as_array(t.bfacets[b], (t.bfacets_count[b], 2)).copy()
+                        if t.bfacets_count[b] else np.zeros((0, 2), np.int32)
+                        for b in range(abi.DES_NBDRY)]
+        self._ptr = ptr
+
+    def boundary_normals(self, mesh, coord, params):
+        _ck(lib().des_boundary_normals(self._ptr, abi.iptr(mesh.connectivity), abi.dptr(coord),
+                                       C.byref(params)), "des_boundary_normals")
+
+    def __del__(self):
+        try:
+            lib().des_topology_free(self._ptr)
+        except Exception:
+            pass
+
+
+class Device:
+    """A device-resident DynEarthSol3D state on one GPU."""
+
+    def __init__(self, mesh, params, device=0):
+        self.L = lib()
+        self.mesh, self.params = mesh, params
+        self.h = C.c_void_p()
+        self._mv = mesh.view()
+        _ck(self.L.des_gpu_create(C.byref(self._mv), C.byref(params), device, C.byref(self.h)),
+            "des_gpu_create")
+
+    def close(self):
+        if self.h:
+            self.L.des_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, params):
+        self.params = params
+        _ck(self.L.des_gpu_set_params(self.h, C.byref(params)), "des_gpu_set_params")
+
+    def upload(self, state, mask=abi.F_ALL):
+        v = state.view()
+        _ck(self.L.des_gpu_upload(self.h, C.byref(v), mask), "des_gpu_upload")
+
+    def download(self, state, mask=abi.F_ALL):
+        v = state.view()
+        _ck(self.L.des_gpu_download(self.h, C.byref(v), mask), "des_gpu_download")
+        state.sync_scalars(v)
+        return state
+
+    def init_fields(self):
+        _ck(self.L.des_gpu_init_fields(self.h), "des_gpu_init_fields")
+
+    def step(self, nsteps=1, report=True):
+        r = abi.StepReport()
+        _ck(self.L.des_gpu_step(self.h, nsteps, C.byref(r) if report else None), "des_gpu_step")
+        return r
+
+    def step_host(self, state, nsteps=1, mask=abi.F_STEP_STATE):
+        r = abi.StepReport()
+        v = state.view()
+        _ck(self.L.des_gpu_step_host(self.h, C.byref(v), mask, nsteps, C.byref(r)),
+            "des_gpu_step_host")
+        state.sync_scalars(v)
+        return r
+
+    def report(self):
+        r = abi.StepReport()
+        _ck(self.L.des_gpu_report(self.h, C.byref(r)), "des_gpu_report")
+        return r
+
+    def call(self, name):
+        if name == "compute_dt":
+            dt = C.c_double()
+            _ck(self.L.des_gpu_compute_dt(self.h, C.byref(dt)), "des_gpu_compute_dt")
+            return dt.value
+        _ck(getattr(self.L, "des_gpu_" + name)(self.h), "des_gpu_" + name)
+
+    def time_steps(self, nsteps):
+        ms = C.c_double()
+        _ck(self.L.des_gpu_time_steps(self.h, nsteps, C.byref(ms)), "des_gpu_time_steps")
+        return ms.value
+
+    def profile_steps(self, nsteps):
+        ms = (C.c_double * 6)()
+        _ck(self.L.des_gpu_profile_steps(self.h, nsteps, ms), "des_gpu_profile_steps")
+        return list(ms)
+
+    @property
+    def kernels_per_step(self):
+        return self.L.des_gpu_kernels_per_step(self.h)
+
+    @property
+    def device_bytes(self):
+        return self.L.des_gpu_device_bytes(self.h)
+
+
+def pin(state):
+    """Page-lock every array of a host State (for asynchronous copies)."""
+    L = lib()
+    for n in State.ARRAYS:
+        a = getattr(state, n)
+        _ck(L.des_host_register(a.ctypes.data, a.nbytes), "des_host_register")
+
+
+def unpin(state):
+    L = lib()
+    for n in State.ARRAYS:
+        L.des_host_unregister(getattr(state, n).ctypes.data)
+
+
+def setup_case(cfg, params=None):
+    """Mesh, params (with boundary normals), initial T and plastic strain."""
+    from . import workload as W
+    L = lib()
+    mesh = W.Mesh(cfg, L)
+    T, pls = W.initial_inputs(cfg, mesh, L)
+    p = params if params is not None else W.make_params(cfg)
+    topo = Topology(mesh)
+    topo.boundary_normals(mesh, mesh.coord, p)
+    return mesh, p, T, pls, topo

@@ -1,0 +1,285 @@
+/*
+ * des_gpu.h -- C ABI of the GB300 (sm_103a) time-step library for the
+ * DynEarthSol3D explicit loop (dynearthsol.cxx:354-394).
+ *
+ * Every pointer in these structs is a plain host pointer into storage laid out
+ * exactly like the reference's Array2D<T,N> (array2d.hpp:86-87: row i starts at
+ * a_ + N*i) or std::vector<double>; the library keeps its own structure-of-arrays
+ * copies in device memory.  No torch or CUDA type appears in any signature.
+ *
+ * Threading: one handle is used by one host thread.  Calls are ordered on the
+ * handle's private CUDA stream; des_gpu_download, des_gpu_step (when it fills a
+ * report) and des_gpu_compute_dt synchronise that stream before returning.
+ *
+ * Errors: every entry point returns 0 (DES_OK) or one of the DES_ERR_* codes.
+ * Where the reference calls std::exit(code) the library returns the same code
+ * (11 for "dt <= 0", geometry.cxx:321-325; 12 for inconsistent topology,
+ * mesh.cxx:1676-1678 and matprops.cxx:516-518; 1 for an unknown rheology or
+ * option, rheology.cxx:641-644, fields.cxx:302-304).
+ */
+#ifndef DES_GPU_H
+#define DES_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DES_MAX_MAT 16
+#define DES_NBDRY   10   /* constants.hpp:37 nbdrytypes */
+
+/* return codes */
+#define DES_OK              0
+#define DES_ERR_OPTION      1   /* unknown rheology / damping / surface option */
+#define DES_ERR_ARG         2   /* bad pointer, size or mask */
+#define DES_ERR_CUDA        3   /* a CUDA runtime call failed */
+#define DES_ERR_NOMEM       4   /* device allocation failed */
+#define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / surface processes / fp32 closure not built */
+#define DES_ERR_SIZE        6   /* size above a fixed limit of the entry point */
+#define DES_ERR_DT         11   /* compute_dt produced dt <= 0 (geometry.cxx:321-325) */
+#define DES_ERR_TOPOLOGY   12   /* a segment is on no element (mesh.cxx:1676-1678) */
+
+/* status bits reported by des_gpu_step (device-side status word) */
+#define DES_STATUS_DT_NONPOSITIVE 0x1u   /* compute_dt gave dt <= 0 */
+#define DES_STATUS_NONFINITE      0x2u   /* NaN/Inf in the coordinates (output.cxx:195-208) */
+#define DES_STATUS_NEG_VOLUME     0x4u   /* an element volume became <= 0 */
+#define DES_STATUS_QL_NOCONV      0x8u   /* QL eigen fallback did not converge in 30 sweeps */
+
+/* rheology codes (matprops.hpp:124-130) */
+#define DES_RH_ELASTIC 1
+#define DES_RH_VISCOUS 2
+#define DES_RH_PLASTIC 4
+#define DES_RH_MAXWELL 3
+#define DES_RH_EP      5
+#define DES_RH_EVP     7
+
+/* arithmetic form of the step */
+#define DES_PREC_FP64 0   /* plain FP64, parity with the reference functions */
+#define DES_PREC_FP32 1   /* FP32 element arithmetic, FP64 coordinates/volumes/shape
+                             derivatives/plastic strain/temperature/dt */
+
+/* field mask for upload / download */
+#define DES_F_COORD        (1u << 0)
+#define DES_F_VEL          (1u << 1)
+#define DES_F_FORCE        (1u << 2)
+#define DES_F_TEMPERATURE  (1u << 3)
+#define DES_F_MASS         (1u << 4)   /* mass, tmass, volume_n */
+#define DES_F_NTMP         (1u << 5)
+#define DES_F_VOLUME       (1u << 6)   /* volume, volume_old */
+#define DES_F_STRESS       (1u << 7)
+#define DES_F_STRAIN       (1u << 8)
+#define DES_F_STRAIN_RATE  (1u << 9)
+#define DES_F_PLSTRAIN     (1u << 10)  /* plstrain, delta_plstrain */
+#define DES_F_DPRESSURE    (1u << 11)
+#define DES_F_EDVOLDT      (1u << 12)
+#define DES_F_SHAPE        (1u << 13)  /* shpdx, shpdy, shpdz */
+#define DES_F_TMP_RESULT   (1u << 14)  /* tmp_result, tmp_result_sg */
+#define DES_F_SCALARS      (1u << 15)  /* time, dt, steps */
+#define DES_F_COORD0       (1u << 16)
+#define DES_F_ALL          0x1ffffu
+/* what one step of the loop reads or writes (the state a drop-in keeps on the host) */
+#define DES_F_STEP_STATE   (DES_F_COORD | DES_F_VEL | DES_F_FORCE | DES_F_TEMPERATURE | \
+                            DES_F_MASS | DES_F_NTMP | DES_F_VOLUME | DES_F_STRESS |       \
+                            DES_F_STRAIN | DES_F_STRAIN_RATE | DES_F_PLSTRAIN |           \
+                            DES_F_DPRESSURE | DES_F_EDVOLDT | DES_F_SHAPE | DES_F_SCALARS)
+
+/* One material property vector of Param::mat (parameters.hpp:187-205).
+ * len is 1 (one value for all materials) or nmat, exactly as the reference's
+ * VectorBase::create accepts (matprops.cxx:509-520); the two lengths give
+ * different averaging (matprops.cxx:436-461). */
+typedef struct des_matvec {
+    int    len;
+    double v[DES_MAX_MAT];
+} des_matvec;
+
+/* The Param and Variables scalars the hot path reads (parameters.hpp:82-206,
+ * 245-256). */
+typedef struct des_params {
+    /* Control */
+    double gravity;
+    double inertial_scaling;
+    double dt_fraction;
+    double fixed_dt;
+    double damping_factor;
+    int    damping_option;
+    int    ref_pressure_option;
+    int    surface_process_option;
+    int    is_quasi_static;
+    int    has_thermal_diffusion;
+    /* BC */
+    double surface_temperature;
+    double winkler_delta_rho;
+    double elastic_foundation_constant;
+    int    has_winkler_foundation;
+    int    has_elastic_foundation;
+    int    has_water_loading;
+    /* Mesh */
+    double zlength;
+    /* Mat */
+    int    rheol_type;
+    int    nmat;
+    int    is_plane_strain;
+    double visc_min, visc_max, tension_max, therm_diff_max;
+    des_matvec rho0, alpha, bulk_modulus, shear_modulus;
+    des_matvec visc_exponent, visc_coefficient, visc_activation_energy;
+    des_matvec heat_capacity, therm_cond;
+    des_matvec pls0, pls1, cohesion0, cohesion1;
+    des_matvec friction_angle0, friction_angle1, dilation_angle0, dilation_angle1;
+    /* Variables (set by init_var / create_boundary_normals) */
+    int    vbc_types[DES_NBDRY];
+    double vbc_values[DES_NBDRY];
+    double max_vbc_val;
+    double compensation_pressure;
+    double bnormals[DES_NBDRY][3];
+    double edge_vectors[DES_NBDRY][DES_NBDRY][3];   /* [i][j], i < j */
+    /* library options */
+    int    precision;           /* DES_PREC_* */
+} des_params;
+
+/* Mesh as the reference holds it after create_new_mesh (parameters.hpp:258-263). */
+typedef struct des_mesh_view {
+    int nnode, nelem, nseg, nmat;
+    const int *connectivity;   /* [nelem][4]  conn_t */
+    const int *segment;        /* [nseg][3]   segment_t */
+    const int *segflag;        /* [nseg]      segflag_t */
+    const int *elemmarkers;    /* [nelem][nmat] rows of int_vec2D (marker counts per material) */
+} des_mesh_view;
+
+/* Host copies of the Variables arrays the loop reads and writes
+ * (parameters.hpp:270-280).  Any pointer not selected by a mask may be NULL. */
+typedef struct des_state_view {
+    int nnode, nelem;
+    double *coord, *vel, *force, *coord0;             /* [nnode][3] */
+    double *temperature, *mass, *tmass, *volume_n;    /* [nnode] */
+    double *ntmp;                                     /* [nnode] */
+    double *volume, *volume_old, *edvoldt;            /* [nelem] */
+    double *plstrain, *delta_plstrain, *dpressure;    /* [nelem] */
+    double *tmp_result_sg;                            /* [nelem] */
+    double *stress, *strain, *strain_rate;            /* [nelem][6] */
+    double *shpdx, *shpdy, *shpdz;                    /* [nelem][4] */
+    double *tmp_result;                               /* [nelem][12] */
+    double time, dt;
+    int    steps;
+} des_state_view;
+
+/* Boundary topology in flat form; arrays are owned by the library. */
+typedef struct des_topology {
+    int       nnode, nelem;
+    unsigned *bcflag;            /* [nnode]      create_boundary_flags (mesh.cxx:1529-1550) */
+    int      *support_offsets;   /* [nnode+1]    create_support (mesh.cxx:1703-1717) as CSR */
+    int      *support_elems;     /* [4*nelem]    ascending element id within a node */
+    int      *support_slots;     /* [4*nelem]    local vertex index of the node in that element */
+    int       bnodes_count[DES_NBDRY];
+    int      *bnodes[DES_NBDRY];      /* create_boundary_nodes (mesh.cxx:1553-1573) */
+    int       bfacets_count[DES_NBDRY];
+    int      *bfacets[DES_NBDRY];     /* [count][2] (element, facet); create_boundary_facets (mesh.cxx:1633-1700) */
+} des_topology;
+
+typedef struct des_step_report {
+    int       steps;
+    double    time;
+    double    dt;
+    unsigned  status;            /* DES_STATUS_* bits accumulated since create/upload */
+    long long ql_fallbacks;      /* elements that took the QL branch of dsyevh3 */
+    long long eigen_solves;      /* elements whose principal stresses were computed */
+} des_step_report;
+
+typedef struct des_gpu des_gpu;
+
+/* ---- host-only set-up (no GPU needed) ---------------------------------- */
+
+/* Builds bcflag, support lists, bnodes and bfacets from connectivity, segment
+ * and segflag, with the reference's ordering.  Replaces create_boundary_flags
+ * (mesh.cxx:1542), create_boundary_nodes (mesh.cxx:1553),
+ * create_boundary_facets (mesh.cxx:1633) and create_support (mesh.cxx:1703);
+ * the facet search is a hash lookup instead of the O(nseg*nelem) scan. */
+int  des_topology_build(const des_mesh_view *mesh, des_topology **out);
+void des_topology_free(des_topology *topo);
+
+/* Outward unit normals of the boundaries and the edge vectors of boundary
+ * pairs, written into params->bnormals / params->edge_vectors.  Replaces
+ * create_boundary_normals (bc.cxx:90-179); returns DES_ERR_OPTION where the
+ * reference exits because a slanted (n0..n3) boundary is curved. */
+int  des_boundary_normals(const des_topology *topo, const int *connectivity,
+                          const double *coord, des_params *params);
+
+/* ---- device handle ---------------------------------------------------- */
+
+/* Allocates the device state for one mesh (replaces allocate_variables,
+ * fields.cxx:13-54) and uploads connectivity, support lists and material
+ * tables.  device < 0 keeps the current device. */
+int  des_gpu_create(const des_mesh_view *mesh, const des_params *params, int device,
+                    des_gpu **out);
+int  des_gpu_destroy(des_gpu *g);
+int  des_gpu_set_params(des_gpu *g, const des_params *params);
+
+/* Host Variables -> device (fields in mask).  Marks nodal masses as current,
+ * so the next step uses them as the reference does after update_mesh. */
+int  des_gpu_upload(des_gpu *g, const des_state_view *host, unsigned mask);
+/* device -> host Variables (fields in mask); synchronises. */
+int  des_gpu_download(des_gpu *g, des_state_view *host, unsigned mask);
+
+/* The init() sequence on the device after the mesh is in place
+ * (dynearthsol.cxx:86-105): coord0 = coord, compute_volume, volume_old = volume,
+ * compute_mass with T = 0, compute_shape_fn, apply_vbcs on zero velocity, then
+ * the lithostatic initial_stress_state (ic.cxx:96-132).  Temperature and
+ * plastic strain are taken from the last upload. */
+int  des_gpu_init_fields(des_gpu *g);
+
+/* Runs nsteps of the loop body dynearthsol.cxx:358-394 (without output,
+ * remeshing, phase changes and hydration, which are no-ops for the supported
+ * options) as one CUDA graph per step.  report may be NULL. */
+int  des_gpu_step(des_gpu *g, int nsteps, des_step_report *report);
+
+/* Drop-in form with host buffers: uploads `mask` fields of host, runs nsteps,
+ * downloads the same fields back.  The host arrays stay authoritative, as in
+ * the reference loop. */
+int  des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
+                       des_step_report *report);
+
+int  des_gpu_report(des_gpu *g, des_step_report *report);
+
+/* ---- per-function entry points (resident state, reference semantics) -- */
+int  des_gpu_update_temperature(des_gpu *g);   /* fields.cxx:108-172 */
+int  des_gpu_update_strain_rate(des_gpu *g);   /* fields.cxx:175-247 */
+int  des_gpu_compute_dvoldt(des_gpu *g);       /* geometry.cxx:117-151 (into ntmp) */
+int  des_gpu_compute_edvoldt(des_gpu *g);      /* geometry.cxx:154-182 (from ntmp) */
+int  des_gpu_update_stress(des_gpu *g);        /* rheology.cxx:513-654 */
+int  des_gpu_NMD_stress(des_gpu *g);           /* geometry.cxx:185-254 */
+int  des_gpu_update_force(des_gpu *g);         /* fields.cxx:312-375 + bc.cxx:503-595 + fields.cxx:250-309 */
+int  des_gpu_update_velocity(des_gpu *g);      /* fields.cxx:378-393 */
+int  des_gpu_apply_vbcs(des_gpu *g);           /* bc.cxx:182-500 */
+int  des_gpu_update_coordinate(des_gpu *g);    /* fields.cxx:396-412 */
+int  des_gpu_compute_volume(des_gpu *g);       /* geometry.cxx:86-114 */
+int  des_gpu_compute_mass(des_gpu *g);         /* geometry.cxx:333-385 */
+int  des_gpu_compute_shape_fn(des_gpu *g);     /* geometry.cxx:388-470 */
+int  des_gpu_update_mesh(des_gpu *g);          /* dynearthsol.cxx:237-261 */
+int  des_gpu_rotate_stress(des_gpu *g);        /* fields.cxx:455-533 */
+int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; also stores dt */
+
+/* ---- measurement (no reference counterpart) ----------------------------- */
+/* Runs nsteps graph launches between two CUDA events on the handle's stream
+ * and returns the elapsed device milliseconds (synchronises). */
+int  des_gpu_time_steps(des_gpu *g, int nsteps, double *ms);
+/* Runs nsteps with the six fused passes launched one by one, an event between
+ * each, and returns the summed milliseconds of every pass in ms[6] (order
+ * N-A, E-B, N-B, E-C, N-C, E-A).  Same results as des_gpu_step. */
+int  des_gpu_profile_steps(des_gpu *g, int nsteps, double ms[6]);
+/* Page-locks (or releases) caller memory so uploads and downloads run as
+ * asynchronous DMA. */
+int  des_host_register(void *ptr, long long bytes);
+int  des_host_unregister(void *ptr);
+/* sizeof of the ABI structs, for binding checks: params, mesh view, state
+ * view, topology, step report */
+void des_abi_sizes(long long out[5]);
+
+/* ---- misc ------------------------------------------------------------- */
+const char *des_gpu_error_string(int code);
+/* bytes of device memory held by the handle */
+long long   des_gpu_device_bytes(const des_gpu *g);
+/* number of kernels one des_gpu_step launches per step */
+int         des_gpu_kernels_per_step(const des_gpu *g);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DES_GPU_H */

@@ -1,0 +1,284 @@
+"""TEST INFRASTRUCTURE -- ctypes wrappers of the two CPU checkers.
+
+  PortOracle  oracle/des_oracle.cpp, a restatement of the reference hot path
+              (built here and on any host by build_oracle())
+  RefOracle   the reference's own functions, compiled from its sources by
+              oracle/ref.mk into oracle/_ref/libdesref.so (only where the
+              reference tree is present)
+
+Both offer the same calls on an abi.State; only tests/, __graft_entry__.smoke()
+and bench.py's CPU baseline use them.
+"""
+import ctypes as C
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ORACLE = Path(__file__).resolve().parent
+ROOT = ORACLE.parent
+sys.path.insert(0, str(ROOT / "dynearthsol-old_gb300"))
+from des_gb300 import abi  # noqa: E402
+
+PORT_LIB = ORACLE / "_build" / "libdes_oracle.so"
+REF_LIB = ORACLE / "_ref" / "libdesref.so"
+REF_SRC = Path(os.environ.get("DES_REFERENCE", "/root/reference"))
+
+FUNCTIONS = ["update_temperature", "update_strain_rate", "compute_dvoldt", "compute_edvoldt",
+             "update_stress", "NMD_stress", "update_force", "update_velocity", "apply_vbcs",
+             "update_coordinate", "compute_volume", "compute_mass", "compute_shape_fn",
+             "update_mesh", "rotate_stress"]
+
+
+def build_oracle(force=False):
+    (ORACLE / "_build").mkdir(exist_ok=True)
+    srcs = [ORACLE / "des_oracle.cpp", ORACLE / "des_oracle_eig.cpp"]
+    deps = srcs + [ORACLE / "des_oracle.h", ROOT / "include" / "des_gpu.h"]
+    if force or not PORT_LIB.exists() or any(d.stat().st_mtime > PORT_LIB.stat().st_mtime
+                                             for d in deps):
+        cmd = ["g++", "-std=c++17", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+               "-o", str(PORT_LIB)] + [str(x) for x in srcs]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("oracle build failed\n" + r.stderr)
+    return PORT_LIB
+
+
+def build_ref(jobs=8):
+    """Compile the reference's sources (only where the reference tree exists)."""
+    if not (REF_SRC / "rheology.cxx").exists():
+        return None
+    cmd = ["make", "-s", "-f", str(ORACLE / "ref.mk"), f"REF={REF_SRC}", f"-j{jobs}"]
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=str(ROOT))
+    if r.returncode:
+        raise RuntimeError("reference build failed\n" + r.stderr[-4000:])
+    return REF_LIB
+
+
+class _Base:
+    def __init__(self, mesh, params):
+        self.mesh, self.params = mesh, params
+
+
+class PortOracle(_Base):
+    _L = None
+
+    @classmethod
+    def lib(cls):
+        if cls._L is None:
+            build_oracle()
+            L = C.CDLL(str(PORT_LIB))
+            P = C.POINTER
+            L.dso_create.argtypes = [P(abi.MeshView), P(abi.Params), P(C.c_void_p)]
+            L.dso_destroy.argtypes = [C.c_void_p]
+            L.dso_destroy.restype = None
+            L.dso_set_params.argtypes = [C.c_void_p, P(abi.Params)]
+            L.dso_init_fields.argtypes = [C.c_void_p, P(abi.StateView)]
+            L.dso_step.argtypes = [C.c_void_p, P(abi.StateView), C.c_int]
+            L.dso_compute_dt.argtypes = [C.c_void_p, P(abi.StateView), P(C.c_double)]
+            for f in FUNCTIONS:
+                getattr(L, "dso_" + f).argtypes = [C.c_void_p, P(abi.StateView)]
+            L.dso_bcflag.argtypes = [C.c_void_p, P(C.c_uint)]
+            L.dso_support.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int)]
+            L.dso_bnodes.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+            L.dso_bfacets.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+            L.dso_boundary_normals.argtypes = [C.c_void_p, P(C.c_double), P(abi.Params)]
+            L.dso_dsyevh3.argtypes = [P(C.c_double)] * 3
+            L.dso_principal_stresses3.argtypes = [P(C.c_double)] * 3
+            L.dso_principal_stresses3.restype = None
+            L.dso_elasto_plastic.argtypes = [C.c_double] * 7 + [P(C.c_double), P(C.c_double),
+                                                                P(C.c_double), P(C.c_int)]
+            L.dso_elasto_plastic.restype = None
+            cls._L = L
+        return cls._L
+
+    def __init__(self, mesh, params):
+        super().__init__(mesh, params)
+        self.L = self.lib()
+        self.h = C.c_void_p()
+        self._mv = mesh.view()
+        rc = self.L.dso_create(C.byref(self._mv), C.byref(params), C.byref(self.h))
+        if rc:
+            raise RuntimeError(f"dso_create failed {rc}")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.dso_destroy(self.h)
+
+    def set_params(self, params):
+        self.params = params
+        self.L.dso_set_params(self.h, C.byref(params))
+
+    def boundary_normals(self, coord, params):
+        rc = self.L.dso_boundary_normals(self.h, abi.dptr(coord), C.byref(params))
+        if rc:
+            raise RuntimeError(f"boundary normals failed {rc}")
+
+    def init_fields(self, state):
+        v = state.view()
+        rc = self.L.dso_init_fields(self.h, C.byref(v))
+        state.sync_scalars(v)
+        if rc:
+            raise RuntimeError(f"dso_init_fields failed {rc}")
+
+    def call(self, name, state):
+        v = state.view()
+        if name == "compute_dt":
+            dt = C.c_double()
+            rc = self.L.dso_compute_dt(self.h, C.byref(v), C.byref(dt))
+            if rc:
+                raise RuntimeError(f"compute_dt failed {rc}")
+            return dt.value
+        rc = getattr(self.L, "dso_" + name)(self.h, C.byref(v))
+        state.sync_scalars(v)
+        if rc:
+            raise RuntimeError(f"dso_{name} failed {rc}")
+
+    def step(self, state, n=1):
+        v = state.view()
+        rc = self.L.dso_step(self.h, C.byref(v), n)
+        state.sync_scalars(v)
+        if rc:
+            raise RuntimeError(f"dso_step failed {rc}")
+
+    def bcflag(self):
+        a = np.zeros(self.mesh.nnode, np.uint32)
+        self.L.dso_bcflag(self.h, abi.uptr(a))
+        return a
+
+    def support(self):
+        off = np.zeros(self.mesh.nnode + 1, np.int32)
+        el = np.zeros(4 * self.mesh.nelem, np.int32)
+        self.L.dso_support(self.h, abi.iptr(off), abi.iptr(el))
+        return off, el
+
+    def bnodes(self, b):
+        n = C.c_int()
+        self.L.dso_bnodes(self.h, b, C.byref(n), None)
+        a = np.zeros(n.value, np.int32)
+        self.L.dso_bnodes(self.h, b, C.byref(n), abi.iptr(a))
+        return a
+
+    def bfacets(self, b):
+        n = C.c_int()
+        self.L.dso_bfacets(self.h, b, C.byref(n), None)
+        a = np.zeros((n.value, 2), np.int32)
+        self.L.dso_bfacets(self.h, b, C.byref(n), abi.iptr(a))
+        return a
+
+
+class RefOracle(_Base):
+    """The reference's own functions (oracle/_ref/libdesref.so)."""
+    _L = None
+
+    @classmethod
+    def available(cls):
+        return REF_LIB.exists()
+
+    @classmethod
+    def lib(cls):
+        if cls._L is None:
+            if not REF_LIB.exists():
+                raise RuntimeError("oracle/_ref/libdesref.so is not built")
+            L = C.CDLL(str(REF_LIB))
+            P = C.POINTER
+            L.dsr_create.argtypes = [P(abi.MeshView), P(abi.Params), P(C.c_void_p)]
+            L.dsr_set_state.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
+            L.dsr_get_state.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
+            L.dsr_init_fields.argtypes = [C.c_void_p, P(abi.StateView)]
+            L.dsr_step.argtypes = [C.c_void_p, C.c_int]
+            L.dsr_compute_dt.argtypes = [C.c_void_p]
+            L.dsr_compute_dt.restype = C.c_double
+            L.dsr_max_vbc_val.argtypes = [C.c_void_p]
+            L.dsr_max_vbc_val.restype = C.c_double
+            L.dsr_compensation_pressure.argtypes = [C.c_void_p]
+            L.dsr_compensation_pressure.restype = C.c_double
+            for f in FUNCTIONS:
+                getattr(L, "dsr_" + f).argtypes = [C.c_void_p]
+            L.dsr_bcflag.argtypes = [C.c_void_p, P(C.c_uint)]
+            L.dsr_support.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int)]
+            L.dsr_bnodes.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+            L.dsr_bfacets.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
+            L.dsr_normals.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+            L.dsr_dsyevh3.argtypes = [P(C.c_double)] * 3
+            cls._L = L
+        return cls._L
+
+    def __init__(self, mesh, params):
+        super().__init__(mesh, params)
+        self.L = self.lib()
+        self.h = C.c_void_p()
+        self._mv = mesh.view()
+        rc = self.L.dsr_create(C.byref(self._mv), C.byref(params), C.byref(self.h))
+        if rc:
+            raise RuntimeError(f"dsr_create failed {rc}")
+
+    def init_fields(self, state):
+        v = state.view()
+        self.L.dsr_init_fields(self.h, C.byref(v))
+        state.sync_scalars(v)
+
+    def _in(self, state):
+        v = state.view()
+        self.L.dsr_set_state(self.h, C.byref(v), abi.F_ALL)
+
+    def _out(self, state):
+        v = state.view()
+        self.L.dsr_get_state(self.h, C.byref(v), abi.F_ALL)
+        state.sync_scalars(v)
+
+    def call(self, name, state):
+        self._in(state)
+        if name == "compute_dt":
+            return self.L.dsr_compute_dt(self.h)
+        getattr(self.L, "dsr_" + name)(self.h)
+        self._out(state)
+
+    def step(self, state, n=1):
+        self._in(state)
+        self.L.dsr_step(self.h, n)
+        self._out(state)
+
+    def bcflag(self):
+        a = np.zeros(self.mesh.nnode, np.uint32)
+        self.L.dsr_bcflag(self.h, abi.uptr(a))
+        return a
+
+    def support(self):
+        off = np.zeros(self.mesh.nnode + 1, np.int32)
+        el = np.zeros(4 * self.mesh.nelem, np.int32)
+        self.L.dsr_support(self.h, abi.iptr(off), abi.iptr(el))
+        return off, el
+
+    def bnodes(self, b):
+        n = C.c_int()
+        self.L.dsr_bnodes(self.h, b, C.byref(n), None)
+        a = np.zeros(n.value, np.int32)
+        self.L.dsr_bnodes(self.h, b, C.byref(n), abi.iptr(a))
+        return a
+
+    def bfacets(self, b):
+        n = C.c_int()
+        self.L.dsr_bfacets(self.h, b, C.byref(n), None)
+        a = np.zeros((n.value, 2), np.int32)
+        self.L.dsr_bfacets(self.h, b, C.byref(n), abi.iptr(a))
+        return a
+
+    def normals(self):
+        bn = np.zeros((10, 3))
+        ev = np.zeros((10, 10, 3))
+        self.L.dsr_normals(self.h, abi.dptr(bn), abi.dptr(ev))
+        return bn, ev
+
+
+def dsyevh3(a, which="port"):
+    """Eigen-decomposition of a 3x3 symmetric matrix (upper part of a)."""
+    a = np.ascontiguousarray(a, np.float64).reshape(9)
+    q = np.zeros(9)
+    w = np.zeros(3)
+    L = PortOracle.lib() if which == "port" else RefOracle.lib()
+    fn = L.dso_dsyevh3 if which == "port" else L.dsr_dsyevh3
+    rc = fn(abi.dptr(a), abi.dptr(q), abi.dptr(w))
+    return rc, q.reshape(3, 3), w

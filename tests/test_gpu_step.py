@@ -1,0 +1,125 @@
+"""The fused, graph-captured time step against the oracle's loop body
+(dynearthsol.cxx:358-394)."""
+import numpy as np
+import pytest
+
+from des_gb300 import abi, workload as W
+from helpers import Case, plastic_config, evp_config, layered_config, rel_l2, diff_fields, COMPARED
+
+_cases = {}
+
+
+def case(name):
+    if name not in _cases:
+        cfg = {"c1": W.CONFIGS["1"], "tiny": W.CONFIGS["tiny"], "plastic": plastic_config(),
+               "evp": evp_config(), "layered": layered_config()}[name]
+        _cases[name] = Case(cfg)
+    return _cases[name]
+
+
+def run_gpu(c, state, nsteps, chunks=1):
+    dev = c.device()
+    dev.upload(state, abi.F_ALL)
+    for _ in range(chunks):
+        rep = dev.step(nsteps // chunks)
+    got = dev.download(abi.State(c.mesh.nnode, c.mesh.nelem), abi.F_ALL)
+    dev.close()
+    return got, rep
+
+
+@pytest.mark.gpu
+def test_config1_2000_steps_bit_identical(gpu):
+    """Config 1 (9,600 tets) for the full 2,000 steps: every field equal."""
+    c = case("c1")
+    s0 = c.initial_state()
+    want = s0.copy()
+    c.oracle.step(want, 2000)
+    got, rep = run_gpu(c, s0, 2000, chunks=4)
+    assert rep.status == 0
+    assert got.steps == want.steps == 2000 and got.dt == want.dt and got.time == want.time
+    bad = diff_fields(got, want)
+    assert not bad, {f: rel_l2(getattr(got, f), getattr(want, f)) for f in bad}
+
+
+# Per-step bar from an identical input state.  Elasto-plastic without
+# yielding: every bit equal.  With yielding, CUDA's atan2/sincos in the
+# eigen-solver differ from the host libm by an ulp, and the return map
+# amplifies that in elements whose trial stress has two close principal
+# values; the strict CPU restatement and the reference's own build (3x3-C
+# with -ffast-math) differ by up to 3e-11 on the same states, so stress,
+# strain and plastic strain are held to 5e-12 there and everything else to
+# 1e-12.  EVP uses CUDA's pow/exp for the viscosity: 1e-12.
+ONE_STEP_TOL = {"tiny": 0.0, "plastic": 5e-12, "evp": 1e-12, "layered": 1e-12}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tiny", "plastic", "evp", "layered"])
+def test_one_step_from_the_same_state(gpu, name):
+    c = case(name)
+    tol = ONE_STEP_TOL[name]
+    for k in [0, 5, 40]:
+        s0 = c.state_after(k)
+        want = s0.copy()
+        c.oracle.step(want, 1)
+        got, rep = run_gpu(c, s0, 1)
+        for f in COMPARED:
+            t = tol if f in ("stress", "strain", "plstrain", "delta_plstrain", "dpressure") else min(tol, 1e-12)
+            assert rel_l2(getattr(got, f), getattr(want, f)) <= t, (k, f, rel_l2(getattr(got, f), getattr(want, f)))
+        for f in ["vel", "temperature"]:
+            assert rel_l2(getattr(got, f), getattr(want, f)) <= 1e-12
+        assert got.dt == want.dt and got.steps == want.steps
+
+
+# After 200 steps: elasto-plastic bit-identical; EVP accumulates the per-step
+# ulp differences of pow/exp in the viscosity (measured 1.2e-9 for velocity
+# on the 3-layer box), held to 1e-8.
+MULTI_TOL = {"tiny": 0.0, "evp": 1e-8, "layered": 1e-8}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tiny", "evp", "layered"])
+def test_multi_step(gpu, name):
+    c = case(name)
+    s0 = c.initial_state()
+    want = s0.copy()
+    c.oracle.step(want, 200)
+    got, rep = run_gpu(c, s0, 200, chunks=2)
+    for f in ["vel", "stress", "temperature"]:
+        assert rel_l2(getattr(got, f), getattr(want, f)) <= MULTI_TOL[name], (f, rel_l2(getattr(got, f), getattr(want, f)))
+
+
+@pytest.mark.gpu
+def test_fused_step_equals_per_function_sequence(gpu):
+    """The six fused passes and the per-function kernels give identical bits."""
+    c = case("plastic")
+    s0 = c.state_after(30)
+    a, _ = run_gpu(c, s0, 1)
+    dev = c.device()
+    dev.upload(s0, abi.F_ALL)
+    s = abi.State(c.mesh.nnode, c.mesh.nelem)
+    # the loop body through the per-function entry points
+    dev.download(s, abi.F_SCALARS)
+    s.steps += 1
+    s.time += s.dt
+    dev.upload(s, abi.F_SCALARS)
+    for fn in ["update_temperature", "update_strain_rate", "compute_dvoldt", "compute_edvoldt",
+               "update_stress", "NMD_stress", "update_force", "update_velocity", "apply_vbcs",
+               "update_mesh", "rotate_stress"]:
+        dev.call(fn)
+    b = dev.download(abi.State(c.mesh.nnode, c.mesh.nelem), abi.F_ALL)
+    dev.close()
+    bad = diff_fields(a, b, [f for f in COMPARED if f not in ("ntmp",)])
+    assert not bad, bad
+
+
+@pytest.mark.gpu
+def test_step_host_round_trip(gpu):
+    """des_gpu_step_host (host buffers in and out) equals upload/step/download."""
+    c = case("tiny")
+    s0 = c.state_after(3)
+    a, _ = run_gpu(c, s0, 2)
+    dev = c.device()
+    b = s0.copy()
+    dev.step_host(b, 2, abi.F_ALL)
+    dev.close()
+    assert not diff_fields(a, b)
