@@ -600,6 +600,14 @@ __device__ __forceinline__ void conduction(const double *dx, const double *dy, c
     }
 }
 
+// geometry.cxx:280-293 for one element: 3 V / (largest facet area)
+__device__ __forceinline__ double min_height(const double X[4][3], double vol)
+{
+    double maxa = smax(smax(tri_area(X[0], X[1], X[2]), tri_area(X[0], X[1], X[3])),
+                       smax(tri_area(X[2], X[3], X[0]), tri_area(X[2], X[3], X[1])));
+    return 3 * vol / maxa;
+}
+
 // orderable 64-bit image of a double (total order for non-NaN values)
 __device__ __forceinline__ unsigned long long order_bits(double x)
 {

@@ -355,14 +355,6 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double 
     }
 }
 
-// geometry.cxx:271-309 for one element: minh and its dt_diffusion candidate
-__device__ __forceinline__ double min_height(const double X[4][3], double vol)
-{
-    double maxa = smax(smax(tri_area(X[0], X[1], X[2]), tri_area(X[0], X[1], X[3])),
-                       smax(tri_area(X[2], X[3], X[0]), tri_area(X[2], X[3], X[1])));
-    return 3 * vol / maxa;
-}
-
 // block-level minimum of two values + the last block turns the global minima
 // into dt (geometry.cxx:311-325).  No thread waits on another block.
 __device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff, bool active)
