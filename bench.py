@@ -87,10 +87,13 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def build_case(cfg_key):
+def build_case(cfg_key, box=None):
     import des_gb300 as D
     from des_gb300 import workload as W
     cfg = W.CONFIGS[cfg_key]
+    if box:
+        nx, ny, nz = (int(v) for v in box.lower().split("x"))
+        cfg = W.scaled(cfg, nx, ny, nz)
     mesh, p, T, pls, topo = D.setup_case(cfg)
     return cfg, mesh, p, T, pls
 
@@ -150,7 +153,7 @@ def run_ours(args):
         tdist.init_process_group("nccl")
 
     D.build()
-    cfg, mesh, p, T, pls = build_case(args.config)
+    cfg, mesh, p, T, pls = build_case(args.config, args.box)
     dev = D.Device(mesh, p, device=local)
     s = W.new_state(mesh, T, pls)
     dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
@@ -259,6 +262,8 @@ def main():
     ap.add_argument("--config", default="2")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
+                    "(profiling of smaller cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
