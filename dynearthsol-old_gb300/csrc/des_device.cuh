@@ -221,7 +221,7 @@ __device__ __forceinline__ void eig_cardano(const double *A, double w[3])
     w[1] -= s;
 }
 
-__device__ __noinline__ int eig_ql(const double *A, double Q[3][3], double w[3])
+static __device__ __noinline__ int eig_ql(const double *A, double Q[3][3], double w[3])
 {
     const double a00 = A[0], a11 = A[1], a22 = A[2], a01 = A[3], a02 = A[4], a12 = A[5];
     double e[3];

@@ -66,6 +66,8 @@ def lib():
     L.des_host_unregister.argtypes = [C.c_void_p]
     L.des_abi_sizes.argtypes = [P(C.c_longlong)]
     L.des_abi_sizes.restype = None
+    L.des_compute_dt_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         P(abi.DtInputs), C.c_void_p, C.c_void_p]
     _lib = L
     return L
 

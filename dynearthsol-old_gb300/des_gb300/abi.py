@@ -128,6 +128,14 @@ class StepReport(C.Structure):
                 ("eigen_solves", C.c_longlong)]
 
 
+class DtInputs(C.Structure):
+    _fields_ = [("visc_min", C.c_double), ("therm_diff_max", C.c_double),
+                ("max_vbc_val", C.c_double), ("inertial_scaling", C.c_double),
+                ("dt_fraction", C.c_double), ("fixed_dt", C.c_double),
+                ("shear_modulus", C.c_double), ("bulkm0", C.c_double), ("rho0", C.c_double),
+                ("is_quasi_static", C.c_int), ("has_thermal_diffusion", C.c_int)]
+
+
 class BoxSpec(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("xlength", C.c_double), ("ylength", C.c_double), ("zlength", C.c_double),

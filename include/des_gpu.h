@@ -256,6 +256,31 @@ int  des_gpu_update_mesh(des_gpu *g);          /* dynearthsol.cxx:237-261 */
 int  des_gpu_rotate_stress(des_gpu *g);        /* fields.cxx:455-533 */
 int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; also stores dt */
 
+/* ---- stable dt without any device allocation ---------------------------- */
+/* Inputs of des_compute_dt_noalloc (the Param / MatProps values compute_dt
+ * reads, geometry.cxx:257-330). */
+typedef struct des_dt_inputs {
+    double visc_min, therm_diff_max, max_vbc_val, inertial_scaling, dt_fraction, fixed_dt;
+    double shear_modulus;   /* every element's shear modulus when shearm is NULL */
+    double bulkm0, rho0;    /* bulkm(0) and rho(0); read only when not quasi-static */
+    int    is_quasi_static, has_thermal_diffusion;
+} des_dt_inputs;
+
+/* No counterpart in the reference: an entry point for callers that cannot
+ * call cudaMalloc (they manage all device memory themselves, or must not let
+ * a library call cudaMalloc/cudaFree, which can synchronise the device).  It
+ * computes the same dt as compute_dt from device arrays the caller passes in
+ * the reference layout -- coord [nnode][3], connectivity [nelem][4] (16-byte
+ * aligned), volume [nelem], optional per-element shear modulus -- and writes
+ * it to the device double *dt, on `stream` (NULL: default stream), without
+ * allocating anything.  Its scratch is a fixed array inside the library:
+ * nelem is limited to 16,777,216 (DES_ERR_SIZE above), calls that overlap on
+ * the GPU race, and the first call on a device does a one-time set-up of the
+ * array's address (make it before any stream capture). */
+int  des_compute_dt_noalloc(int nelem, const double *coord, const int *connectivity,
+                            const double *volume, const double *shearm,
+                            const des_dt_inputs *in, double *dt, void *stream);
+
 /* ---- measurement (no reference counterpart) ----------------------------- */
 /* Runs nsteps graph launches between two CUDA events on the handle's stream
  * and returns the elapsed device milliseconds (synchronises). */
