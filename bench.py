@@ -87,6 +87,25 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
+def replica_throughput(ms, nelem, steps, world, reduce_max=None):
+    """Whole-job element-steps/s of `world` independent replicas: every rank
+    processed nelem * steps element-steps; the job took the slowest rank's time."""
+    if reduce_max is not None:
+        ms = reduce_max(ms)
+    return world * nelem * steps / (ms / 1e3), ms
+
+
+def torch_reduce_max(device):
+    import torch
+    import torch.distributed as tdist
+
+    def f(ms):
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item())
+    return f
+
+
 def build_case(cfg_key, box=None):
     import des_gb300 as D
     from des_gb300 import workload as W
@@ -168,12 +187,9 @@ def run_ours(args):
     with ClockSampler(local) as clk:
         ms = dev.time_steps(args.steps)
     barrier()
-    if dist:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{local}")
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
+    value, ms = replica_throughput(ms, mesh.nelem, args.steps, world,
+                                   torch_reduce_max(f"cuda:{local}") if dist else None)
     rep = dev.report()
-    value = world * mesh.nelem * args.steps / (ms / 1e3)
 
     # per-pass device times over extra steps (same arithmetic, launched one by one)
     prof_steps = max(2, min(args.steps, 5))

@@ -1,0 +1,91 @@
+"""The CPU restatement against the reference's own functions compiled from
+its sources (oracle/_ref).  Runs where the reference tree is present."""
+import numpy as np
+import pytest
+
+from des_gb300 import abi, workload as W
+from helpers import Case, plastic_config, evp_config, layered_config, rel_l2, diff_fields, COMPARED, LOOP
+from oracle.oracle import RefOracle, dsyevh3
+
+pytestmark = pytest.mark.skipif(not RefOracle.available(), reason="reference build absent")
+
+
+def both(cfg):
+    c = Case(cfg)
+    r = RefOracle(c.mesh, c.params)
+    return c, r
+
+
+def test_config1_init_and_2000_steps_bit_exact():
+    c, r = both(W.CONFIGS["1"])
+    a = W.new_state(c.mesh, c.T, c.pls)
+    b = W.new_state(c.mesh, c.T, c.pls)
+    c.oracle.init_fields(a)
+    r.init_fields(b)
+    assert not diff_fields(a, b) and a.dt == b.dt
+    c.oracle.step(a, 2000)
+    r.step(b, 2000)
+    assert not diff_fields(a, b)
+    assert (a.time, a.dt, a.steps) == (b.time, b.dt, b.steps)
+
+
+@pytest.mark.parametrize("key", ["evp", "layered"])
+def test_evp_and_layered_200_steps_bit_exact(key):
+    c, r = both(evp_config() if key == "evp" else layered_config())
+    a = W.new_state(c.mesh, c.T, c.pls)
+    b = W.new_state(c.mesh, c.T, c.pls)
+    c.oracle.init_fields(a)
+    r.init_fields(b)
+    c.oracle.step(a, 200)
+    r.step(b, 200)
+    assert not diff_fields(a, b)
+
+
+@pytest.mark.parametrize("fn", LOOP + ["update_coordinate", "compute_volume", "compute_mass",
+                                      "compute_shape_fn"])
+def test_every_function_bit_exact_on_a_loop_state(fn):
+    c, r = both(W.CONFIGS["tiny"])
+    s = c.state_before(fn, 7) if fn != "update_mesh" else c.state_before("update_mesh", 7)
+    a, b = s.copy(), s.copy()
+    c.oracle.call(fn, a)
+    r.call(fn, b)
+    assert not diff_fields(a, b)
+
+
+def test_compute_dt_bit_exact():
+    c, r = both(plastic_config())
+    s = c.state_after(20)
+    assert c.oracle.call("compute_dt", s.copy()) == r.call("compute_dt", s.copy())
+
+
+def test_yielding_state_per_step_tolerance():
+    """Only the eigen-solver differs: the reference builds 3x3-C with
+    -O3 -ffast-math.  From identical yielding states one step differs by at most
+    1e-10 (relative L2), everything without an eigen-solve is bit-exact."""
+    c, r = both(plastic_config())
+    for k in (10, 40):
+        s = c.state_after(k)
+        a, b = s.copy(), s.copy()
+        c.oracle.step(a, 1)
+        r.step(b, 1)
+        for f in COMPARED:
+            assert rel_l2(getattr(a, f), getattr(b, f)) <= 1e-10, (k, f)
+
+
+def test_eigen_solver_on_well_separated_spectra():
+    """Spectra with gaps >= 1e6 in [-1e8, 1e8]: the strict restatement and the
+    reference's fast-math build agree to 1e-9 of the scale (Cardano's
+    tr^2 - 3 c1 cancellation makes both carry errors of that order when a
+    common offset dominates; the strict one is the closer to the exact
+    eigenvalues; both are within 1e-7 of the exact ones)."""
+    rng = np.random.default_rng(5)
+    for _ in range(2000):
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        w = np.sort(rng.uniform(-1e8, 1e8, 3))
+        if np.min(np.diff(w)) < 1e6:
+            continue
+        a = np.triu(q @ np.diag(w) @ q.T)
+        _, q1, w1 = dsyevh3(a, "port")
+        _, q2, w2 = dsyevh3(a, "ref")
+        assert np.abs(w1 - w2).max() <= 1e-9 * np.abs(w2).max()
+        assert np.abs(np.sort(w1) - w).max() <= 1e-7 * np.abs(w).max()
