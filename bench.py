@@ -173,16 +173,23 @@ def run_ours(args):
 
     D.build()
     cfg, mesh, p, T, pls = build_case(args.config, args.box)
-    dev = D.Device(mesh, p, device=local)
-    s = W.new_state(mesh, T, pls)
-    dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
-    dev.init_fields()
-    dev.step(args.warmup)                       # warm-up (also captures the graph)
 
     def barrier():
         if dist:
             tdist.barrier()
 
+    def make_form(precision):
+        q = abi.Params.from_buffer_copy(p)
+        q.precision = precision
+        dv = D.Device(mesh, q, device=local)
+        s0 = W.new_state(mesh, T, pls)
+        dv.upload(s0, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dv.init_fields()
+        dv.step(args.warmup)                       # warm-up (also captures the graph)
+        return dv
+
+    # FP64 plain form: the headline
+    dev = make_form(abi.PREC_FP64)
     barrier()
     with ClockSampler(local) as clk:
         ms = dev.time_steps(args.steps)
@@ -190,6 +197,46 @@ def run_ours(args):
     value, ms = replica_throughput(ms, mesh.nelem, args.steps, world,
                                    torch_reduce_max(f"cuda:{local}") if dist else None)
     rep = dev.report()
+    S = dev.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+
+    def rel(a, b):
+        nb = float(np.linalg.norm(b))
+        return float(np.linalg.norm(a - b) / (nb if nb else 1.0))
+
+    def compare(x, y):
+        return {f: rel(getattr(x, f), getattr(y, f))
+                for f in ("vel", "force", "stress", "strain", "temperature", "coord")}
+
+    # FP32 mixed form: timed on the same workload, then checked from the FP64
+    # state S (one step, and 100 steps) against the FP64 form
+    forms = {"fp64_plain": {"value": value, "ms_per_step": ms / args.steps}}
+    dev32 = make_form(abi.PREC_FP32)
+    barrier()
+    with ClockSampler(local) as clk32:
+        ms32 = dev32.time_steps(args.steps)
+    barrier()
+    v32, ms32 = replica_throughput(ms32, mesh.nelem, args.steps, world,
+                                   torch_reduce_max(f"cuda:{local}") if dist else None)
+    prof32 = max(2, min(args.steps, 5))
+    passes32 = dev32.profile_steps(prof32)
+    rep32 = dev32.report()
+    errs = {}
+    for nsteps in (1, 100):
+        dev.upload(S, abi.F_ALL)
+        dev.step(nsteps)
+        a = dev.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+        dev32.upload(S, abi.F_ALL)
+        dev32.step(nsteps)
+        b = dev32.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+        errs[f"after_{nsteps}_steps"] = compare(b, a)
+    dev32.close()
+    dev.upload(S, abi.F_ALL)
+    forms["fp32_mixed"] = {
+        "value": v32, "ms_per_step": ms32 / args.steps, "speedup_vs_fp64": v32 / value,
+        "rel_l2_vs_fp64_from_the_same_state": errs,
+        "passes_ms_per_step": dict(zip(["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"],
+                                       [t / prof32 for t in passes32])),
+        "eigen_solves": rep32.eigen_solves, "clocks": clk32.summary()}
 
     # per-pass device times over extra steps (same arithmetic, launched one by one)
     prof_steps = max(2, min(args.steps, 5))
@@ -255,6 +302,7 @@ def run_ours(args):
                      "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm},
         "passes_ms_per_step": {n: t / prof_steps for n, t in zip(names, per_pass)},
+        "forms": forms,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
                 "d2h_bytes_per_step": io_bytes},
         "clocks": clk.summary(),

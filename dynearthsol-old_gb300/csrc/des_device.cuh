@@ -51,22 +51,28 @@ struct MatTable {
 
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
-__device__ __forceinline__ double tr3(const double *s) { return s[0] + s[1] + s[2]; }
+// The templated helpers below are instantiated with double for the FP64 form
+// (identical operation order to the reference) and with float for the FP32
+// form; literals are cast to R so that a float instantiation stays in FP32.
+template <class R>
+__device__ __forceinline__ R tr3(const R *s) { return s[0] + s[1] + s[2]; }
 
 // utils.hpp:78-87
-__device__ __forceinline__ double second_invariant2(const double *t)
+template <class R>
+__device__ __forceinline__ R second_invariant2(const R *t)
 {
-    double a = (t[0] + t[1] + t[2]) / 3;
-    return (0.5 * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a)) +
+    R a = (t[0] + t[1] + t[2]) / R(3);
+    return (R(0.5) * ((t[0] - a) * (t[0] - a) + (t[1] - a) * (t[1] - a) + (t[2] - a) * (t[2] - a)) +
             t[3] * t[3] + t[4] * t[4] + t[5] * t[5]);
 }
 
 // ---- MatProps -------------------------------------------------------------
 
 // element mean temperature (matprops.cxx:613-618)
-__device__ __forceinline__ double elem_mean4(double a, double b, double c, double d)
+template <class R>
+__device__ __forceinline__ R elem_mean4(R a, R b, R c, R d)
 {
-    double t = 0;
+    R t = 0;
     t += a;
     t += b;
     t += c;
@@ -383,31 +389,32 @@ __device__ __forceinline__ int principal3(const double *s, double p[3], double v
 
 // ---- rheology (rheology.cxx:108-302, 3D) ----------------------------------
 
-__device__ __forceinline__ void elastic(double bulkm, double shearm, const double *de, double *s)
+template <class R>
+__device__ __forceinline__ void elastic(R bulkm, R shearm, const R *de, R *s)
 {
-    double lambda = bulkm - 2. / 3 * shearm;
-    double dev = tr3(de);
+    R lambda = bulkm - R(2.) / R(3) * shearm;
+    R dev = tr3(de);
     for (int i = 0; i < 3; ++i) s[i] += 2 * shearm * de[i] + lambda * dev;
     for (int i = 3; i < 6; ++i) s[i] += 2 * shearm * de[i];
 }
 
-__device__ __forceinline__ void maxwell(double bulkm, double shearm, double viscosity, double dt,
-                                        double dv, const double *de, double *s)
+template <class R>
+__device__ __forceinline__ void maxwell(R bulkm, R shearm, R viscosity, R dt, R dv, const R *de, R *s)
 {
-    double tmp = 0.5 * dt * shearm / viscosity;
-    double f1 = 1 - tmp;
-    double f2 = 1 / (1 + tmp);
-    double dev = tr3(de) / 3;
-    double s0 = tr3(s) / 3;
+    R tmp = R(0.5) * dt * shearm / viscosity;
+    R f1 = 1 - tmp;
+    R f2 = 1 / (1 + tmp);
+    R dev = tr3(de) / 3;
+    R s0 = tr3(s) / 3;
     for (int i = 0; i < 3; ++i)
         s[i] = ((s[i] - s0) * f1 + 2 * shearm * (de[i] - dev)) * f2 + s0 + bulkm * dv;
     for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + 2 * shearm * de[i]) * f2;
 }
 
-__device__ __forceinline__ void viscous(double bulkm, double viscosity, double total_dv,
-                                        const double *edot, double *s)
+template <class R>
+__device__ __forceinline__ void viscous(R bulkm, R viscosity, R total_dv, const R *edot, R *s)
 {
-    double dev = tr3(edot) / 3;
+    R dev = tr3(edot) / 3;
     for (int i = 0; i < 3; ++i) s[i] = 2 * viscosity * (edot[i] - dev) + bulkm * total_dv;
     for (int i = 3; i < 6; ++i) s[i] = 2 * viscosity * edot[i];
 }
@@ -546,8 +553,8 @@ __device__ __forceinline__ void shape_fn(const double X[4][3], double vol, doubl
 }
 
 // fields.cxx:193-241: D = sym(grad v) from the four nodal velocities V[i][d]
-__device__ __forceinline__ void strain_rate(const double V[4][3], const double *dx, const double *dy,
-                                            const double *dz, double *s)
+template <class R>
+__device__ __forceinline__ void strain_rate(const R V[4][3], const R *dx, const R *dy, const R *dz, R *s)
 {
     s[0] = 0;
     for (int i = 0; i < 4; ++i) s[0] += V[i][0] * dx[i];
@@ -556,32 +563,34 @@ __device__ __forceinline__ void strain_rate(const double V[4][3], const double *
     s[2] = 0;
     for (int i = 0; i < 4; ++i) s[2] += V[i][2] * dz[i];
     s[3] = 0;
-    for (int i = 0; i < 4; ++i) s[3] += 0.5 * (V[i][0] * dy[i] + V[i][1] * dx[i]);
+    for (int i = 0; i < 4; ++i) s[3] += R(0.5) * (V[i][0] * dy[i] + V[i][1] * dx[i]);
     s[4] = 0;
-    for (int i = 0; i < 4; ++i) s[4] += 0.5 * (V[i][0] * dz[i] + V[i][2] * dx[i]);
+    for (int i = 0; i < 4; ++i) s[4] += R(0.5) * (V[i][0] * dz[i] + V[i][2] * dx[i]);
     s[5] = 0;
-    for (int i = 0; i < 4; ++i) s[5] += 0.5 * (V[i][1] * dz[i] + V[i][2] * dy[i]);
+    for (int i = 0; i < 4; ++i) s[5] += R(0.5) * (V[i][1] * dz[i] + V[i][2] * dy[i]);
 }
 
 // fields.cxx:483-504: spin components
-__device__ __forceinline__ void spin(const double V[4][3], const double *dx, const double *dy,
-                                     const double *dz, double &w3, double &w4, double &w5)
+template <class R>
+__device__ __forceinline__ void spin(const R V[4][3], const R *dx, const R *dy, const R *dz, R &w3,
+                                     R &w4, R &w5)
 {
     w3 = 0;
-    for (int i = 0; i < 4; ++i) w3 += 0.5 * (V[i][0] * dy[i] - V[i][1] * dx[i]);
+    for (int i = 0; i < 4; ++i) w3 += R(0.5) * (V[i][0] * dy[i] - V[i][1] * dx[i]);
     w4 = 0;
-    for (int i = 0; i < 4; ++i) w4 += 0.5 * (V[i][0] * dz[i] - V[i][2] * dx[i]);
+    for (int i = 0; i < 4; ++i) w4 += R(0.5) * (V[i][0] * dz[i] - V[i][2] * dx[i]);
     w5 = 0;
-    for (int i = 0; i < 4; ++i) w5 += 0.5 * (V[i][1] * dz[i] - V[i][2] * dy[i]);
+    for (int i = 0; i < 4; ++i) w5 += R(0.5) * (V[i][1] * dz[i] - V[i][2] * dy[i]);
 }
 
 // fields.cxx:419-433
-__device__ __forceinline__ void jaumann(double *s, double dt, double w3, double w4, double w5)
+template <class R>
+__device__ __forceinline__ void jaumann(R *s, R dt, R w3, R w4, R w5)
 {
-    double inc[6];
-    inc[0] = -2.0 * s[3] * w3 - 2.0 * s[4] * w4;
-    inc[1] = 2.0 * s[3] * w3 - 2.0 * s[5] * w5;
-    inc[2] = 2.0 * s[4] * w4 + 2.0 * s[5] * w5;
+    R inc[6];
+    inc[0] = R(-2.0) * s[3] * w3 - R(2.0) * s[4] * w4;
+    inc[1] = R(2.0) * s[3] * w3 - R(2.0) * s[5] * w5;
+    inc[2] = R(2.0) * s[4] * w4 + R(2.0) * s[5] * w5;
     inc[3] = s[0] * w3 - s[1] * w3 - s[4] * w5 - s[5] * w4;
     inc[4] = s[0] * w4 - s[2] * w4 + s[3] * w5 - s[5] * w3;
     inc[5] = s[1] * w5 - s[2] * w5 + s[3] * w4 + s[4] * w3;

@@ -11,7 +11,7 @@
 #include <vector>
 
 #include "des_gpu.h"
-#include "des_kernels.cuh"
+#include "des_kernels32.cuh"
 
 using namespace des;
 
@@ -41,6 +41,10 @@ struct des_gpu {
     long long staging_elems = 0;
     cudaGraphExec_t graph = nullptr;
     bool primed = false;
+    int prec = DES_PREC_FP64;
+    DevF f;
+    ConstsF hF;
+    ConstsF *dF = nullptr;
     bool stress_bcs = false;
     int bfacets_count[DES_NBDRY] = {0};
 };
@@ -107,7 +111,7 @@ int check_params(const des_params &p, int nmat)
         return DES_ERR_OPTION;
     if (p.damping_option < 0 || p.damping_option > 4) return DES_ERR_OPTION;
     if (p.ref_pressure_option != 0 && p.gravity != 0) return DES_ERR_UNSUPPORTED;
-    if (p.precision != DES_PREC_FP64) return DES_ERR_UNSUPPORTED;
+    if (p.precision != DES_PREC_FP64 && p.precision != DES_PREC_FP32) return DES_ERR_UNSUPPORTED;
     const des_matvec *vs[] = {&p.rho0, &p.alpha, &p.bulk_modulus, &p.shear_modulus,
                               &p.visc_exponent, &p.visc_coefficient, &p.visc_activation_energy,
                               &p.heat_capacity, &p.therm_cond, &p.pls0, &p.pls1, &p.cohesion0,
@@ -222,6 +226,68 @@ int build_consts(des_gpu *g)
     if (cudaMemcpyAsync(g->dK, &g->hK, sizeof(Consts), cudaMemcpyHostToDevice, g->stream) !=
         cudaSuccess)
         return DES_ERR_CUDA;
+    if (g->dF) {
+        ConstsF &F = g->hF;
+        std::memset(&F, 0, sizeof(F));
+        F.nmat = M.nmat;
+        F.nmix = M.nmix;
+        for (int i = 0; i < M.nmix; ++i) {
+            const Mix &x = M.mix[i];
+            MixF &y = F.mix[i];
+            y.bulkm = (float)x.bulkm;
+            y.shearm = (float)x.shearm;
+            y.cp = (float)x.cp;
+            y.k = (float)x.k;
+            y.rho_qs = (float)x.rho_qs;
+            double rr = 0, ra = 0;
+            int nn = 0;
+            for (int m = 0; m < M.nmat; ++m) {
+                rr += M.rho0[m] * x.count[m];
+                ra += M.rho0[m] * M.alpha[m] * x.count[m];
+                nn += x.count[m];
+            }
+            y.rho_ref = rr / nn;
+            y.rho_alpha = (float)(ra / nn);
+            y.single = x.single;
+            y.n = x.n;
+            for (int m = 0; m < kMaxMat; ++m) y.count[m] = x.count[m];
+        }
+        for (int m = 0; m < M.nmat; ++m) {
+            F.rho0[m] = (float)M.rho0[m];
+            F.alpha[m] = (float)M.alpha[m];
+            F.vexp_pw[m] = (float)M.vexp_pw[m];
+            F.vlog_coef[m] = (float)std::log(0.25 * M.vcoef_pow[m] * 1e6);
+            F.vQ[m] = (float)M.vQ[m];
+            F.vnR[m] = (float)M.vnR[m];
+            F.pls0[m] = (float)M.pls0[m];
+            F.pls1[m] = (float)M.pls1[m];
+            F.c0[m] = (float)M.c0[m];
+            F.c1[m] = (float)M.c1[m];
+            F.f0[m] = (float)M.f0[m];
+            F.f1[m] = (float)M.f1[m];
+            F.d0[m] = (float)M.d0[m];
+            F.d1[m] = (float)M.d1[m];
+            F.hslope[m] = (float)M.hslope[m];
+        }
+        F.phi_c = (float)M.phi_c;
+        F.anphi_c = (float)M.anphi_c;
+        F.sqanphi_c = (float)M.sqanphi_c;
+        F.tphi_c = (float)M.tphi_c;
+        F.psi_c = (float)M.psi_c;
+        F.anpsi_c = (float)M.anpsi_c;
+        F.visc_min = (float)M.visc_min;
+        F.visc_max = (float)M.visc_max;
+        F.tension_max = (float)M.tension_max;
+        F.gravity = (float)p.gravity;
+        F.surface_temperature = (float)p.surface_temperature;
+        F.therm_diff_max = (float)p.therm_diff_max;
+        F.rheol = p.rheol_type;
+        F.thermal = K.thermal;
+        F.is_qs = K.is_qs;
+        if (cudaMemcpyAsync(g->dF, &g->hF, sizeof(ConstsF), cudaMemcpyHostToDevice, g->stream) !=
+            cudaSuccess)
+            return DES_ERR_CUDA;
+    }
     return cudaStreamSynchronize(g->stream) == cudaSuccess ? DES_OK : DES_ERR_CUDA;
 }
 
@@ -255,6 +321,35 @@ int download_field(des_gpu *g, double *host, const double *src, int ncomp, long 
     return DES_OK;
 }
 
+int upload_field(des_gpu *g, const double *host, float *dst, int ncomp, long long rows)
+{
+    if (!host) return DES_ERR_ARG;
+    long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
+    for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
+        long long nr = std::min(chunk_rows, rows - r0);
+        DES_CUDA(cudaMemcpyAsync(g->staging, host + r0 * ncomp, sizeof(double) * nr * ncomp,
+                                 cudaMemcpyHostToDevice, g->stream));
+        k_aos_to_soa_f<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(g->staging, dst, ncomp, nr,
+                                                                         r0, rows);
+        DES_LAUNCH();
+    }
+    return DES_OK;
+}
+int download_field(des_gpu *g, double *host, const float *src, int ncomp, long long rows)
+{
+    if (!host) return DES_ERR_ARG;
+    long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
+    for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
+        long long nr = std::min(chunk_rows, rows - r0);
+        k_soa_to_aos_f<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(src, g->staging, ncomp, nr,
+                                                                         r0, rows);
+        DES_LAUNCH();
+        DES_CUDA(cudaMemcpyAsync(host + r0 * ncomp, g->staging, sizeof(double) * nr * ncomp,
+                                 cudaMemcpyDeviceToHost, g->stream));
+    }
+    return DES_OK;
+}
+
 int read_clock(des_gpu *g, Clock &c)
 {
     DES_CUDA(cudaMemcpyAsync(&c, g->dclk, sizeof(Clock), cudaMemcpyDeviceToHost, g->stream));
@@ -271,11 +366,70 @@ int begin_fn(des_gpu *g)
     int rc = read_clock(g, c);
     if (rc) return rc;
     if (!c.mass_valid) {
-        k_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
+        if (g->prec == DES_PREC_FP32)
+            kf_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->f);
+        else
+            k_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
         DES_LAUNCH();
     }
     g->primed = false;
     return DES_OK;
+}
+
+// the per-function entry points operate on the FP64 form's fields
+int begin_fn64(des_gpu *g)
+{
+    if (!g) return DES_ERR_ARG;
+    if (g->prec != DES_PREC_FP64) return DES_ERR_UNSUPPORTED;
+    return begin_fn(g);
+}
+
+int prime(des_gpu *g)
+{
+    if (g->primed) return DES_OK;
+    if (g->prec == DES_PREC_FP32)
+        kf_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->f);
+    else
+        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
+    DES_LAUNCH();
+    g->primed = true;
+    return DES_OK;
+}
+
+// the six passes of one step, in order, on g's stream (captured or not)
+void launch_step(des_gpu *g, cudaEvent_t *ev)
+{
+    const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
+    cudaStream_t st = g->stream;
+    if (ev) cudaEventRecord(ev[0], st);
+    if (g->prec == DES_PREC_FP32) {
+        const DevF &f = g->f;
+        kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f);
+        if (ev) cudaEventRecord(ev[1], st);
+        kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
+        if (ev) cudaEventRecord(ev[2], st);
+        kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f);
+        if (ev) cudaEventRecord(ev[3], st);
+        kf_fe_c<<<eb, kElemBlock, 0, st>>>(f);
+        if (ev) cudaEventRecord(ev[4], st);
+        kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f);
+        if (ev) cudaEventRecord(ev[5], st);
+        kf_fe_a<<<eb, kElemBlock, 0, st>>>(f);
+    } else {
+        const Dev &d = g->d;
+        k_fn_a<<<nb, kNodeBlock, 0, st>>>(d);
+        if (ev) cudaEventRecord(ev[1], st);
+        k_fe_b<<<eb, kElemBlock, 0, st>>>(d);
+        if (ev) cudaEventRecord(ev[2], st);
+        k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d);
+        if (ev) cudaEventRecord(ev[3], st);
+        k_fe_c<<<eb, kElemBlock, 0, st>>>(d);
+        if (ev) cudaEventRecord(ev[4], st);
+        k_fn_c<<<nb, kNodeBlock, 0, st>>>(d);
+        if (ev) cudaEventRecord(ev[5], st);
+        k_fe_a<<<eb, kElemBlock, 0, st>>>(d);
+    }
+    if (ev) cudaEventRecord(ev[6], st);
 }
 
 int finish(des_gpu *g)
@@ -287,16 +441,9 @@ int finish(des_gpu *g)
 
 int capture_step_graph(des_gpu *g)
 {
-    const Dev &d = g->d;
     cudaGraph_t graph;
     DES_CUDA(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
-    const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
-    k_fn_a<<<nb, kNodeBlock, 0, g->stream>>>(d);
-    k_fe_b<<<eb, kElemBlock, 0, g->stream>>>(d);
-    k_sg_gather<<<nb, kNodeBlock, 0, g->stream>>>(d);
-    k_fe_c<<<eb, kElemBlock, 0, g->stream>>>(d);
-    k_fn_c<<<nb, kNodeBlock, 0, g->stream>>>(d);
-    k_fe_a<<<eb, kElemBlock, 0, g->stream>>>(d);
+    launch_step(g, nullptr);
     cudaError_t e = cudaStreamEndCapture(g->stream, &graph);
     if (e != cudaSuccess) return DES_ERR_CUDA;
     e = cudaGraphInstantiate(&g->graph, graph, 0);
@@ -397,37 +544,25 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess)
         return fail(DES_ERR_CUDA);
     const size_t N = m->nnode, E = m->nelem;
+    g->prec = p->precision;
     Dev &d = g->d;
     d.nnode = m->nnode;
     d.nelem = m->nelem;
-    double *coord, *vel, *force, *coord0;
+    double *coord, *coord0;
     int4 *conn;
     int *sup_off;
     unsigned *sup_ent, *bcflag;
     unsigned char *dmix;
-    if ((rc = dev_alloc(g, &coord, 3 * N)) || (rc = dev_alloc(g, &vel, 3 * N)) ||
-        (rc = dev_alloc(g, &force, 3 * N)) || (rc = dev_alloc(g, &coord0, 3 * N)) ||
-        (rc = dev_alloc(g, &d.T, N)) || (rc = dev_alloc(g, &d.mass, N)) ||
-        (rc = dev_alloc(g, &d.tmass, N)) || (rc = dev_alloc(g, &d.vol_n, N)) ||
-        (rc = dev_alloc(g, &d.ntmp, N)) || (rc = dev_alloc(g, &bcflag, N)) ||
+    // arrays both forms keep in FP64 (and the topology)
+    if ((rc = dev_alloc(g, &coord, 3 * N)) || (rc = dev_alloc(g, &coord0, 3 * N)) ||
+        (rc = dev_alloc(g, &d.T, N)) || (rc = dev_alloc(g, &bcflag, N)) ||
         (rc = dev_alloc(g, &sup_off, N + 1)) || (rc = dev_alloc(g, &sup_ent, 4 * E)) ||
         (rc = dev_alloc(g, &conn, E)) || (rc = dev_alloc(g, &dmix, E)) ||
         (rc = dev_alloc(g, &d.vol, E)) || (rc = dev_alloc(g, &d.vol_old, E)) ||
-        (rc = dev_alloc(g, &d.edvoldt, E)) || (rc = dev_alloc(g, &d.pls, E)) ||
-        (rc = dev_alloc(g, &d.dpls, E)) || (rc = dev_alloc(g, &d.dp, E)) ||
-        (rc = dev_alloc(g, &d.tmp_sg, E)) || (rc = dev_alloc(g, &d.stress, 6 * E)) ||
-        (rc = dev_alloc(g, &d.strain, 6 * E)) || (rc = dev_alloc(g, &d.srate, 6 * E)) ||
-        (rc = dev_alloc(g, &d.srate_next, 6 * E)) || (rc = dev_alloc(g, &d.shp, 12 * E)) ||
-        (rc = dev_alloc(g, &d.tmp, 12 * E)) || (rc = dev_alloc(g, &d.c_mass, E)) ||
-        (rc = dev_alloc(g, &d.c_tmass, E)) || (rc = dev_alloc(g, &d.c_trdv, E)) ||
-        (rc = dev_alloc(g, &g->dK, 1)) || (rc = dev_alloc(g, &g->dclk, 1)))
+        (rc = dev_alloc(g, &d.pls, E)) || (rc = dev_alloc(g, &g->dK, 1)) ||
+        (rc = dev_alloc(g, &g->dclk, 1)))
         return fail(rc);
-    g->staging_elems = std::min<long long>(12LL * (long long)E, 1LL << 25);
-    g->staging_elems = std::max<long long>(g->staging_elems, 3LL * (long long)N < (1LL << 25) ? 3LL * (long long)N : (1LL << 25));
-    if ((rc = dev_alloc(g, &g->staging, (size_t)g->staging_elems))) return fail(rc);
     d.x = coord; d.y = coord + N; d.z = coord + 2 * N;
-    d.vx = vel; d.vy = vel + N; d.vz = vel + 2 * N;
-    d.fx = force; d.fy = force + N; d.fz = force + 2 * N;
     d.x0 = coord0; d.y0 = coord0 + N; d.z0 = coord0 + 2 * N;
     d.conn = conn;
     d.sup_off = sup_off;
@@ -436,6 +571,59 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     d.mix = dmix;
     d.K = g->dK;
     d.clk = g->dclk;
+    if (g->prec == DES_PREC_FP64) {
+        double *vel, *force;
+        if ((rc = dev_alloc(g, &vel, 3 * N)) || (rc = dev_alloc(g, &force, 3 * N)) ||
+            (rc = dev_alloc(g, &d.mass, N)) || (rc = dev_alloc(g, &d.tmass, N)) ||
+            (rc = dev_alloc(g, &d.vol_n, N)) || (rc = dev_alloc(g, &d.ntmp, N)) ||
+            (rc = dev_alloc(g, &d.edvoldt, E)) || (rc = dev_alloc(g, &d.dpls, E)) ||
+            (rc = dev_alloc(g, &d.dp, E)) || (rc = dev_alloc(g, &d.tmp_sg, E)) ||
+            (rc = dev_alloc(g, &d.stress, 6 * E)) || (rc = dev_alloc(g, &d.strain, 6 * E)) ||
+            (rc = dev_alloc(g, &d.srate, 6 * E)) || (rc = dev_alloc(g, &d.srate_next, 6 * E)) ||
+            (rc = dev_alloc(g, &d.shp, 12 * E)) || (rc = dev_alloc(g, &d.tmp, 12 * E)) ||
+            (rc = dev_alloc(g, &d.c_mass, E)) || (rc = dev_alloc(g, &d.c_tmass, E)) ||
+            (rc = dev_alloc(g, &d.c_trdv, E)))
+            return fail(rc);
+        d.vx = vel; d.vy = vel + N; d.vz = vel + 2 * N;
+        d.fx = force; d.fy = force + N; d.fz = force + 2 * N;
+    } else {
+        DevF &f = g->f;
+        float *vel, *force;
+        if ((rc = dev_alloc(g, &vel, 3 * N)) || (rc = dev_alloc(g, &force, 3 * N)) ||
+            (rc = dev_alloc(g, &f.mass, N)) || (rc = dev_alloc(g, &f.tmass, N)) ||
+            (rc = dev_alloc(g, &f.vol_n, N)) || (rc = dev_alloc(g, &f.ntmp, N)) ||
+            (rc = dev_alloc(g, &f.edvoldt, E)) || (rc = dev_alloc(g, &f.dpls, E)) ||
+            (rc = dev_alloc(g, &f.dp, E)) || (rc = dev_alloc(g, &f.tmp_sg, E)) ||
+            (rc = dev_alloc(g, &f.stress, 6 * E)) || (rc = dev_alloc(g, &f.strain, 6 * E)) ||
+            (rc = dev_alloc(g, &f.srate, 6 * E)) || (rc = dev_alloc(g, &f.srate_next, 6 * E)) ||
+            (rc = dev_alloc(g, &f.shp, 12 * E)) || (rc = dev_alloc(g, &f.tmp, 12 * E)) ||
+            (rc = dev_alloc(g, &f.c_vol, E)) || (rc = dev_alloc(g, &f.c_mass, E)) ||
+            (rc = dev_alloc(g, &f.c_tmass, E)) || (rc = dev_alloc(g, &f.c_trdv, E)) ||
+            (rc = dev_alloc(g, &f.s0, E)) || (rc = dev_alloc(g, &f.f0, 12 * E)) ||
+            (rc = dev_alloc(g, &g->dF, 1)))
+            return fail(rc);
+        f.nnode = d.nnode;
+        f.nelem = d.nelem;
+        f.conn = conn;
+        f.sup_off = sup_off;
+        f.sup_ent = sup_ent;
+        f.bcflag = bcflag;
+        f.mix = dmix;
+        f.x = d.x; f.y = d.y; f.z = d.z;
+        f.x0 = d.x0; f.y0 = d.y0; f.z0 = d.z0;
+        f.T = d.T;
+        f.vol = d.vol;
+        f.vol_old = d.vol_old;
+        f.pls = d.pls;
+        f.vx = vel; f.vy = vel + N; f.vz = vel + 2 * N;
+        f.fx = force; f.fy = force + N; f.fz = force + 2 * N;
+        f.K = g->dK;
+        f.F = g->dF;
+        f.clk = g->dclk;
+    }
+    g->staging_elems = std::min<long long>(12LL * (long long)E, 1LL << 25);
+    g->staging_elems = std::max<long long>(g->staging_elems, 3LL * (long long)N < (1LL << 25) ? 3LL * (long long)N : (1LL << 25));
+    if ((rc = dev_alloc(g, &g->staging, (size_t)g->staging_elems))) return fail(rc);
 
     std::vector<unsigned> ent(4 * E);
     for (size_t q = 0; q < 4 * E; ++q)
@@ -475,6 +663,7 @@ int des_gpu_set_params(des_gpu *g, const des_params *p)
     if (!g || !p) return DES_ERR_ARG;
     int rc = check_params(*p, g->nmat);
     if (rc) return rc;
+    if (p->precision != g->prec) return DES_ERR_ARG;   // the device layout depends on it
     g->P = *p;
     g->primed = false;
     return build_consts(g);
@@ -490,32 +679,62 @@ int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
     const long long N = g->nnode, E = g->nelem;
     Dev &d = g->d;
     int rc = DES_OK;
+    const bool f32 = g->prec == DES_PREC_FP32;
+    DevF &f = g->f;
 #define UP(flag, ptr, dst, nc, rows) \
     if ((mask & (flag)) && (rc = upload_field(g, h->ptr, dst, nc, rows))) return rc;
+    // fields of the form's precision (FP32 copies in the mixed form)
+#define UPX(flag, ptr, fld, off, nc, rows)                                                    \
+    if (mask & (flag)) {                                                                     \
+        rc = f32 ? upload_field(g, h->ptr, f.fld + (off), nc, rows)                          \
+                 : upload_field(g, h->ptr, d.fld + (off), nc, rows);                         \
+        if (rc) return rc;                                                                   \
+    }
     UP(DES_F_COORD, coord, d.x, 3, N)
     UP(DES_F_COORD0, coord0, d.x0, 3, N)
-    UP(DES_F_VEL, vel, d.vx, 3, N)
-    UP(DES_F_FORCE, force, d.fx, 3, N)
+    UPX(DES_F_VEL, vel, vx, 0, 3, N)
+    UPX(DES_F_FORCE, force, fx, 0, 3, N)
     UP(DES_F_TEMPERATURE, temperature, d.T, 1, N)
-    UP(DES_F_MASS, mass, d.mass, 1, N)
-    UP(DES_F_MASS, tmass, d.tmass, 1, N)
-    UP(DES_F_MASS, volume_n, d.vol_n, 1, N)
-    UP(DES_F_NTMP, ntmp, d.ntmp, 1, N)
+    UPX(DES_F_MASS, mass, mass, 0, 1, N)
+    UPX(DES_F_MASS, tmass, tmass, 0, 1, N)
+    UPX(DES_F_MASS, volume_n, vol_n, 0, 1, N)
+    UPX(DES_F_NTMP, ntmp, ntmp, 0, 1, N)
     UP(DES_F_VOLUME, volume, d.vol, 1, E)
     UP(DES_F_VOLUME, volume_old, d.vol_old, 1, E)
-    UP(DES_F_STRESS, stress, d.stress, 6, E)
-    UP(DES_F_STRAIN, strain, d.strain, 6, E)
-    UP(DES_F_STRAIN_RATE, strain_rate, d.srate, 6, E)
+    if (mask & DES_F_STRESS) {
+        if (f32) {
+            if (!h->stress) return DES_ERR_ARG;
+            long long chunk = std::max(1LL, g->staging_elems / 6);
+            for (long long r0 = 0; r0 < E; r0 += chunk) {
+                long long nr = std::min(chunk, E - r0);
+                DES_CUDA(cudaMemcpyAsync(g->staging, h->stress + 6 * r0, sizeof(double) * 6 * nr,
+                                         cudaMemcpyHostToDevice, g->stream));
+                k_stress_split<<<blocks(nr, 256), 256, 0, g->stream>>>(g->staging, f.s0, f.stress, nr,
+                                                                        r0, E);
+                DES_LAUNCH();
+            }
+        } else if ((rc = upload_field(g, h->stress, d.stress, 6, E))) {
+            return rc;
+        }
+    }
+    UPX(DES_F_STRAIN, strain, strain, 0, 6, E)
+    UPX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     UP(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
-    UP(DES_F_PLSTRAIN, delta_plstrain, d.dpls, 1, E)
-    UP(DES_F_DPRESSURE, dpressure, d.dp, 1, E)
-    UP(DES_F_EDVOLDT, edvoldt, d.edvoldt, 1, E)
-    UP(DES_F_SHAPE, shpdx, d.shp, 4, E)
-    UP(DES_F_SHAPE, shpdy, d.shp + 4 * E, 4, E)
-    UP(DES_F_SHAPE, shpdz, d.shp + 8 * E, 4, E)
-    UP(DES_F_TMP_RESULT, tmp_result, d.tmp, 12, E)
-    UP(DES_F_TMP_RESULT, tmp_result_sg, d.tmp_sg, 1, E)
+    UPX(DES_F_PLSTRAIN, delta_plstrain, dpls, 0, 1, E)
+    UPX(DES_F_DPRESSURE, dpressure, dp, 0, 1, E)
+    UPX(DES_F_EDVOLDT, edvoldt, edvoldt, 0, 1, E)
+    UPX(DES_F_SHAPE, shpdx, shp, 0, 4, E)
+    UPX(DES_F_SHAPE, shpdy, shp, 4 * E, 4, E)
+    UPX(DES_F_SHAPE, shpdz, shp, 8 * E, 4, E)
+    UPX(DES_F_TMP_RESULT, tmp_result, tmp, 0, 12, E)
+    UPX(DES_F_TMP_RESULT, tmp_result_sg, tmp_sg, 0, 1, E)
 #undef UP
+#undef UPX
+    if (f32 && (mask & DES_F_VOLUME)) {
+        // FP32 copy of the volumes used as element weights
+        k_vol_to_f<<<blocks(E, 256), 256, 0, g->stream>>>(d.vol, f.c_vol, E);
+        DES_LAUNCH();
+    }
     if (mask & (DES_F_SCALARS | DES_F_MASS)) {
         Clock c;
         if ((rc = read_clock(g, c))) return rc;
@@ -541,36 +760,63 @@ int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
     Clock c;
     int rc = read_clock(g, c);
     if (rc) return rc;
+    const bool f32 = g->prec == DES_PREC_FP32;
+    DevF &f = g->f;
     if ((mask & DES_F_MASS) && !c.mass_valid) {
-        k_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(d);
+        if (f32)
+            kf_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(f);
+        else
+            k_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(d);
         DES_LAUNCH();
     }
 #define DOWN(flag, ptr, src, nc, rows) \
     if ((mask & (flag)) && (rc = download_field(g, h->ptr, src, nc, rows))) return rc;
+#define DOWNX(flag, ptr, fld, off, nc, rows)                                                  \
+    if (mask & (flag)) {                                                                     \
+        rc = f32 ? download_field(g, h->ptr, f.fld + (off), nc, rows)                        \
+                 : download_field(g, h->ptr, d.fld + (off), nc, rows);                       \
+        if (rc) return rc;                                                                   \
+    }
     DOWN(DES_F_COORD, coord, d.x, 3, N)
     DOWN(DES_F_COORD0, coord0, d.x0, 3, N)
-    DOWN(DES_F_VEL, vel, d.vx, 3, N)
-    DOWN(DES_F_FORCE, force, d.fx, 3, N)
+    DOWNX(DES_F_VEL, vel, vx, 0, 3, N)
+    DOWNX(DES_F_FORCE, force, fx, 0, 3, N)
     DOWN(DES_F_TEMPERATURE, temperature, d.T, 1, N)
-    DOWN(DES_F_MASS, mass, d.mass, 1, N)
-    DOWN(DES_F_MASS, tmass, d.tmass, 1, N)
-    DOWN(DES_F_MASS, volume_n, d.vol_n, 1, N)
-    DOWN(DES_F_NTMP, ntmp, d.ntmp, 1, N)
+    DOWNX(DES_F_MASS, mass, mass, 0, 1, N)
+    DOWNX(DES_F_MASS, tmass, tmass, 0, 1, N)
+    DOWNX(DES_F_MASS, volume_n, vol_n, 0, 1, N)
+    DOWNX(DES_F_NTMP, ntmp, ntmp, 0, 1, N)
     DOWN(DES_F_VOLUME, volume, d.vol, 1, E)
     DOWN(DES_F_VOLUME, volume_old, d.vol_old, 1, E)
-    DOWN(DES_F_STRESS, stress, d.stress, 6, E)
-    DOWN(DES_F_STRAIN, strain, d.strain, 6, E)
-    DOWN(DES_F_STRAIN_RATE, strain_rate, d.srate, 6, E)
+    if (mask & DES_F_STRESS) {
+        if (f32) {
+            if (!h->stress) return DES_ERR_ARG;
+            long long chunk = std::max(1LL, g->staging_elems / 6);
+            for (long long r0 = 0; r0 < E; r0 += chunk) {
+                long long nr = std::min(chunk, E - r0);
+                k_stress_join<<<blocks(nr, 256), 256, 0, g->stream>>>(f.s0, f.stress, g->staging, nr,
+                                                                       r0, E);
+                DES_LAUNCH();
+                DES_CUDA(cudaMemcpyAsync(h->stress + 6 * r0, g->staging, sizeof(double) * 6 * nr,
+                                         cudaMemcpyDeviceToHost, g->stream));
+            }
+        } else if ((rc = download_field(g, h->stress, d.stress, 6, E))) {
+            return rc;
+        }
+    }
+    DOWNX(DES_F_STRAIN, strain, strain, 0, 6, E)
+    DOWNX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     DOWN(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
-    DOWN(DES_F_PLSTRAIN, delta_plstrain, d.dpls, 1, E)
-    DOWN(DES_F_DPRESSURE, dpressure, d.dp, 1, E)
-    DOWN(DES_F_EDVOLDT, edvoldt, d.edvoldt, 1, E)
-    DOWN(DES_F_SHAPE, shpdx, d.shp, 4, E)
-    DOWN(DES_F_SHAPE, shpdy, d.shp + 4 * E, 4, E)
-    DOWN(DES_F_SHAPE, shpdz, d.shp + 8 * E, 4, E)
-    DOWN(DES_F_TMP_RESULT, tmp_result, d.tmp, 12, E)
-    DOWN(DES_F_TMP_RESULT, tmp_result_sg, d.tmp_sg, 1, E)
+    DOWNX(DES_F_PLSTRAIN, delta_plstrain, dpls, 0, 1, E)
+    DOWNX(DES_F_DPRESSURE, dpressure, dp, 0, 1, E)
+    DOWNX(DES_F_EDVOLDT, edvoldt, edvoldt, 0, 1, E)
+    DOWNX(DES_F_SHAPE, shpdx, shp, 0, 4, E)
+    DOWNX(DES_F_SHAPE, shpdy, shp, 4 * E, 4, E)
+    DOWNX(DES_F_SHAPE, shpdz, shp, 8 * E, 4, E)
+    DOWNX(DES_F_TMP_RESULT, tmp_result, tmp, 0, 12, E)
+    DOWNX(DES_F_TMP_RESULT, tmp_result_sg, tmp_sg, 0, 1, E)
 #undef DOWN
+#undef DOWNX
     if (mask & DES_F_SCALARS) {
         h->time = c.time;
         h->dt = c.dt;
@@ -598,11 +844,7 @@ int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)
 {
     if (!g || nsteps < 0) return DES_ERR_ARG;
     if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
-    if (!g->primed) {
-        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
-        DES_LAUNCH();
-        g->primed = true;
-    }
+    if (int rc = prime(g)) return rc;
     if (!g->graph) {
         int rc = capture_step_graph(g);
         if (rc) return rc;
@@ -619,11 +861,7 @@ int des_gpu_time_steps(des_gpu *g, int nsteps, double *ms)
 {
     if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
     if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
-    if (!g->primed) {
-        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
-        DES_LAUNCH();
-        g->primed = true;
-    }
+    if (int rc = prime(g)) return rc;
     if (!g->graph) {
         int rc = capture_step_graph(g);
         if (rc) return rc;
@@ -648,31 +886,13 @@ int des_gpu_profile_steps(des_gpu *g, int nsteps, double ms[6])
 {
     if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
     if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
-    if (!g->primed) {
-        k_prime<<<blocks(g->nelem, kElemBlock), kElemBlock, 0, g->stream>>>(g->d);
-        DES_LAUNCH();
-        g->primed = true;
-    }
+    if (int rc = prime(g)) return rc;
     cudaEvent_t ev[7];
     for (int i = 0; i < 7; ++i) DES_CUDA(cudaEventCreate(&ev[i]));
     for (int k = 0; k < 6; ++k) ms[k] = 0;
-    const Dev &d = g->d;
-    const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
     DES_CUDA(cudaStreamSynchronize(g->stream));
     for (int s = 0; s < nsteps; ++s) {
-        cudaEventRecord(ev[0], g->stream);
-        k_fn_a<<<nb, kNodeBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[1], g->stream);
-        k_fe_b<<<eb, kElemBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[2], g->stream);
-        k_sg_gather<<<nb, kNodeBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[3], g->stream);
-        k_fe_c<<<eb, kElemBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[4], g->stream);
-        k_fn_c<<<nb, kNodeBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[5], g->stream);
-        k_fe_a<<<eb, kElemBlock, 0, g->stream>>>(d);
-        cudaEventRecord(ev[6], g->stream);
+        launch_step(g, ev);
         DES_LAUNCH();
         DES_CUDA(cudaEventSynchronize(ev[6]));
         for (int k = 0; k < 6; ++k) {
@@ -719,7 +939,7 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
 
 int des_gpu_update_temperature(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_temp_elem<<<ELEM_GRID(g)>>>(g->d);
     k_temp_node<<<NODE_GRID(g)>>>(g->d);
@@ -727,14 +947,14 @@ int des_gpu_update_temperature(des_gpu *g)
 }
 int des_gpu_update_strain_rate(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_srate<<<ELEM_GRID(g)>>>(g->d, g->d.srate);
     return finish(g);
 }
 int des_gpu_compute_dvoldt(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_dvoldt_elem<<<ELEM_GRID(g)>>>(g->d);
     k_sg_gather<<<NODE_GRID(g)>>>(g->d);
@@ -742,21 +962,21 @@ int des_gpu_compute_dvoldt(des_gpu *g)
 }
 int des_gpu_compute_edvoldt(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_edvoldt<<<ELEM_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_update_stress(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_stress<<<ELEM_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_NMD_stress(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_dp_elem<<<ELEM_GRID(g)>>>(g->d);
     k_sg_gather<<<NODE_GRID(g)>>>(g->d);
@@ -765,7 +985,7 @@ int des_gpu_NMD_stress(des_gpu *g)
 }
 int des_gpu_update_force(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     k_force_elem<<<ELEM_GRID(g)>>>(g->d);
@@ -774,35 +994,35 @@ int des_gpu_update_force(des_gpu *g)
 }
 int des_gpu_update_velocity(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_velocity<<<NODE_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_apply_vbcs(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_vbcs<<<NODE_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_update_coordinate(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_coord<<<NODE_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_compute_volume(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_volume<<<ELEM_GRID(g)>>>(g->d, 0);
     return finish(g);
 }
 int des_gpu_compute_mass(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_mass_elem<<<ELEM_GRID(g)>>>(g->d, g->d.T);
     k_mass_node<<<NODE_GRID(g)>>>(g->d);
@@ -811,14 +1031,14 @@ int des_gpu_compute_mass(des_gpu *g)
 }
 int des_gpu_compute_shape_fn(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_shape<<<ELEM_GRID(g)>>>(g->d);
     return finish(g);
 }
 int des_gpu_update_mesh(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_coord<<<NODE_GRID(g)>>>(g->d);
     k_volume<<<ELEM_GRID(g)>>>(g->d, 1);
@@ -830,7 +1050,7 @@ int des_gpu_update_mesh(des_gpu *g)
 }
 int des_gpu_rotate_stress(des_gpu *g)
 {
-    int rc = begin_fn(g);
+    int rc = begin_fn64(g);
     if (rc) return rc;
     k_rotate<<<ELEM_GRID(g)>>>(g->d);
     return finish(g);
@@ -851,9 +1071,41 @@ int des_gpu_compute_dt(des_gpu *g, double *dt_out)
     return (c.dt > 0) ? DES_OK : DES_ERR_DT;
 }
 
+static int init_fields_fp32(des_gpu *g)
+{
+    const size_t N = g->nnode, E = g->nelem;
+    DevF &f = g->f;
+    cudaStream_t s = g->stream;
+    g->primed = false;
+    DES_CUDA(cudaMemsetAsync(f.vx, 0, sizeof(float) * 3 * N, s));
+    DES_CUDA(cudaMemsetAsync(f.fx, 0, sizeof(float) * 3 * N, s));
+    DES_CUDA(cudaMemsetAsync(f.stress, 0, sizeof(float) * 6 * E, s));
+    DES_CUDA(cudaMemsetAsync(f.s0, 0, sizeof(double) * E, s));
+    DES_CUDA(cudaMemsetAsync(f.strain, 0, sizeof(float) * 6 * E, s));
+    DES_CUDA(cudaMemsetAsync(f.srate, 0, sizeof(float) * 6 * E, s));
+    DES_CUDA(cudaMemcpyAsync(f.x0, f.x, sizeof(double) * 3 * N, cudaMemcpyDeviceToDevice, s));
+    kf_init_geometry<<<ELEM_GRID(g)>>>(f);
+    kf_mass_flush<<<NODE_GRID(g)>>>(f);
+    k_clock_set<<<1, 32, 0, s>>>(g->dclk, 0.0, 0.0, 0, 1);
+    kf_vbcs<<<NODE_GRID(g)>>>(f);
+    if (g->P.gravity != 0) kf_init_stress<<<ELEM_GRID(g)>>>(f);
+    return DES_OK;
+}
+
 int des_gpu_init_fields(des_gpu *g)
 {
     if (!g) return DES_ERR_ARG;
+    if (g->prec == DES_PREC_FP32) {
+        int rc = init_fields_fp32(g);
+        if (rc) return rc;
+        g->P.compensation_pressure = g->P.gravity != 0 ? g->P.rho0.v[0] * g->P.gravity * g->P.zlength : 0;
+        g->hK.compensation_pressure = g->P.compensation_pressure;
+        DES_CUDA(cudaMemcpyAsync(&g->dK->compensation_pressure, &g->hK.compensation_pressure,
+                                 sizeof(double), cudaMemcpyHostToDevice, g->stream));
+        if ((rc = finish(g))) return rc;
+        double dt;
+        return des_gpu_compute_dt(g, &dt);
+    }
     const size_t N = g->nnode, E = g->nelem;
     Dev &d = g->d;
     g->primed = false;

@@ -208,20 +208,22 @@ __device__ __forceinline__ void count_eigen(const Dev &d, int flags)
 }
 
 // fields.cxx:264-297 for one component
-__device__ __forceinline__ double damp(const Consts &K, double f, double v)
+template <class R>
+__device__ __forceinline__ R damp(const Consts &K, R f, R v)
 {
+    const R fac = R(K.damping_factor);
     switch (K.damping_option) {
     case 1:
-        if (fabs(v) > 1e-13) f -= K.damping_factor * copysign(f, v);
+        if (fabs(v) > R(1e-13)) f -= fac * copysign(f, v);
         break;
     case 2:
-        f -= K.damping_factor * f;
+        f -= fac * f;
         break;
     case 3:
         if ((f < 0) == (v < 0))
-            f -= K.damping_factor * f;
+            f -= fac * f;
         else
-            f += (1 - K.damping_factor) * f;
+            f += (1 - fac) * f;
         break;
     default:
         break;
@@ -230,13 +232,14 @@ __device__ __forceinline__ double damp(const Consts &K, double f, double v)
 }
 
 // bc.cxx:201-496 for one node
-__device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double v[3])
+template <class R>
+__device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, R v[3])
 {
     if (!(flag & kBoundAny)) return;
     const int vx0 = K.vbc_types[0], vx1 = K.vbc_types[1], vy0 = K.vbc_types[2],
               vy1 = K.vbc_types[3], vz0 = K.vbc_types[4], vz1 = K.vbc_types[5];
-    const double ux0 = K.vbc_values[0], ux1 = K.vbc_values[1], uy0 = K.vbc_values[2],
-                 uy1 = K.vbc_values[3], uz0 = K.vbc_values[4], uz1 = K.vbc_values[5];
+    const R ux0 = R(K.vbc_values[0]), ux1 = R(K.vbc_values[1]), uy0 = R(K.vbc_values[2]),
+            uy1 = R(K.vbc_values[3]), uz0 = R(K.vbc_values[4]), uz1 = R(K.vbc_values[5]);
     if (flag & kBoundX0) {
         switch (vx0) {
         case 1: v[0] = ux0; break;
@@ -280,24 +283,26 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double 
     if (flag & 0x3c0u) {
         for (int ib = 6; ib <= 9; ib++) {
             if (!(flag & (1u << ib))) continue;
-            const double *n = K.bnormals[ib];
-            double fac = 0;
+            const R n[3] = {R(K.bnormals[ib][0]), R(K.bnormals[ib][1]), R(K.bnormals[ib][2])};
+            const R val = R(K.vbc_values[ib]);
+            R fac = 0;
             switch (K.vbc_types[ib]) {
             case 1:
                 if (flag == (1u << ib)) {
-                    double vn = 0;
+                    R vn = 0;
                     for (int dd = 0; dd < 3; dd++) vn += v[dd] * n[dd];
-                    for (int dd = 0; dd < 3; dd++) v[dd] += (K.vbc_values[ib] - vn) * n[dd];
+                    for (int dd = 0; dd < 3; dd++) v[dd] += (val - vn) * n[dd];
                 } else {
                     for (int ic = 0; ic < ib; ic++) {
                         if (!(flag & (1u << ic))) continue;
                         if (K.vbc_types[ic] == 0) {
-                            double vn = 0;
+                            R vn = 0;
                             for (int dd = 0; dd < 3; dd++) vn += v[dd] * n[dd];
-                            for (int dd = 0; dd < 3; dd++) v[dd] += (K.vbc_values[ib] - vn) * n[dd];
+                            for (int dd = 0; dd < 3; dd++) v[dd] += (val - vn) * n[dd];
                         } else if (K.vbc_types[ic] == 1) {
-                            const double *edge = K.edge[ic][ib];
-                            double ve = 0;
+                            const R edge[3] = {R(K.edge[ic][ib][0]), R(K.edge[ic][ib][1]),
+                                               R(K.edge[ic][ib][2])};
+                            R ve = 0;
                             for (int dd = 0; dd < 3; dd++) ve += v[dd] * edge[dd];
                             for (int dd = 0; dd < 3; dd++) v[dd] = ve * edge[dd];
                         }
@@ -305,25 +310,25 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double 
                 }
                 break;
             case 3:
-                for (int dd = 0; dd < 3; dd++) v[dd] = K.vbc_values[ib] * n[dd];
+                for (int dd = 0; dd < 3; dd++) v[dd] = val * n[dd];
                 break;
             case 11:
                 fac = 1 / sqrt(1 - n[2] * n[2]);
                 if (flag == (1u << ib)) {
-                    double vn = 0;
+                    R vn = 0;
                     for (int dd = 0; dd < 2; dd++) vn += v[dd] * n[dd];
-                    for (int dd = 0; dd < 2; dd++) v[dd] += (K.vbc_values[ib] * fac - vn) * n[dd];
+                    for (int dd = 0; dd < 2; dd++) v[dd] += (val * fac - vn) * n[dd];
                 } else {
                     for (int ic = 0; ic < ib; ic++) {
                         if (!(flag & (1u << ic))) continue;
                         if (K.vbc_types[ic] == 0) {
-                            double vn = 0;
+                            R vn = 0;
                             for (int dd = 0; dd < 2; dd++) vn += v[dd] * n[dd];
-                            for (int dd = 0; dd < 2; dd++)
-                                v[dd] += (K.vbc_values[ib] * fac - vn) * n[dd];
+                            for (int dd = 0; dd < 2; dd++) v[dd] += (val * fac - vn) * n[dd];
                         } else if (K.vbc_types[ic] == 1) {
-                            const double *edge = K.edge[ic][ib];
-                            double ve = 0;
+                            const R edge[3] = {R(K.edge[ic][ib][0]), R(K.edge[ic][ib][1]),
+                                               R(K.edge[ic][ib][2])};
+                            R ve = 0;
                             for (int dd = 0; dd < 3; dd++) ve += v[dd] * edge[dd];
                             for (int dd = 0; dd < 3; dd++) v[dd] = ve * edge[dd];
                         }
@@ -332,7 +337,7 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, double 
                 break;
             case 13:
                 fac = 1 / sqrt(1 - n[2] * n[2]);
-                for (int dd = 0; dd < 2; dd++) v[dd] = K.vbc_values[ib] * fac * n[dd];
+                for (int dd = 0; dd < 2; dd++) v[dd] = val * fac * n[dd];
                 v[2] = 0;
                 break;
             }

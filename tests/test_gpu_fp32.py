@@ -1,0 +1,151 @@
+"""The FP32 mixed-precision form against the FP64 oracle.
+
+FP64 is kept for coordinates, volumes, shape-derivative evaluation, plastic
+strain, temperature and dt (plus the isotropic reference stress and its force
+contribution); the rest is FP32, with the exact FP64 return map for elements
+the FP32 yield bound cannot prove elastic.
+
+The reference's default damping (option 1, fields.cxx:264-273) switches on the
+sign of every velocity component, which makes the velocity trajectory amplify
+any difference: in pure FP64, a 1e-12 relative change of the initial stress
+grows to 6e-2 in velocity after 2,000 steps of config 1.  So the bars are:
+one step from the same state (tight); 2,000 steps with smooth damping
+(option 2, where the same perturbation stays bounded) at 1e-4; and, with
+option 1, the trajectory error no larger than the FP64 loop's own response to
+a perturbation of the size of FP32 rounding."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import des_gb300 as D
+from des_gb300 import abi, workload as W
+from helpers import Case, plastic_config, evp_config, layered_config, rel_l2
+
+_cases = {}
+
+
+def case(name):
+    if name not in _cases:
+        cfg = {"c1": W.CONFIGS["1"], "evp": evp_config(), "layered": layered_config(),
+               "plastic": plastic_config()}[name]
+        _cases[name] = Case(cfg)
+    return _cases[name]
+
+
+def fp32_params(c):
+    p = abi.Params.from_buffer_copy(c.params)
+    p.precision = abi.PREC_FP32
+    return p
+
+
+def run_fp32(c, s0, nsteps, from_init=False):
+    dev = D.Device(c.mesh, fp32_params(c), device=0)
+    if from_init:
+        s = W.new_state(c.mesh, c.T, c.pls)
+        dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dev.init_fields()
+    else:
+        dev.upload(s0, abi.F_ALL)
+    rep = dev.step(nsteps) if nsteps else None
+    got = dev.download(abi.State(c.mesh.nnode, c.mesh.nelem), abi.F_ALL)
+    dev.close()
+    return got, rep
+
+
+@pytest.mark.gpu
+def test_fp32_init_matches_fp64():
+    c = case("c1")
+    want = c.initial_state()
+    got, _ = run_fp32(c, None, 0, from_init=True)
+    assert got.dt == want.dt
+    for f in ["volume", "coord", "temperature", "plstrain"]:
+        assert np.array_equal(getattr(got, f), getattr(want, f)), f
+    for f in ["stress", "strain", "mass", "tmass", "volume_n", "shpdx", "vel"]:
+        assert rel_l2(getattr(got, f), getattr(want, f)) <= 1e-6, f
+
+
+# Elasto-visco-plastic elements take the Maxwell stress when its second
+# invariant is the smaller (rheology.cxx:630-638).  Where stress and strain
+# increment are both isotropic the two invariants are equal in exact
+# arithmetic and the reference's FP64 choice is decided by rounding residues
+# of about 1e-9 Pa; the two branches then differ in pressure by 3 K (dv - tr de),
+# up to 1e-4 of the local stress.  The FP32 form decides those ties
+# consistently (an exact closed form of the difference) but cannot reproduce
+# the reference's noise, hence the wider EVP bars.
+ONE_STEP = {"c1": dict(vel=1e-6, stress=1e-6, force=1e-6),
+            "evp": dict(vel=1e-3, stress=1e-5, force=1e-5),
+            "layered": dict(vel=1e-3, stress=1e-5, force=1e-5)}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1", "evp", "layered"])
+def test_fp32_one_step_from_the_same_state(name):
+    c = case(name)
+    for k in (0, 50):
+        s0 = c.state_after(k)
+        want = s0.copy()
+        c.oracle.step(want, 1)
+        got, _ = run_fp32(c, s0, 1)
+        errs = {f: rel_l2(getattr(got, f), getattr(want, f))
+                for f in ["vel", "force", "stress", "strain", "temperature", "coord"]}
+        for f, tol in ONE_STEP[name].items():
+            assert errs[f] <= tol, (k, errs)
+        assert errs["temperature"] <= 1e-12 and errs["coord"] <= 1e-12, (k, errs)
+
+
+def smooth(cfg):
+    d = dict(cfg.__dict__)
+    d["extra"] = dict(cfg.extra, params=dict(cfg.extra.get("params", {}), damping_option=2))
+    return W.Config(**d)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["c1", "evp"])
+def test_fp32_2000_steps_within_1e4_with_smooth_damping(name):
+    c = Case(smooth(W.CONFIGS["1"] if name == "c1" else evp_config()))
+    s0 = c.initial_state()
+    want = s0.copy()
+    c.oracle.step(want, 2000)
+    got, rep = run_fp32(c, s0, 2000)
+    assert rep.status == 0 and got.steps == 2000
+    errs = {f: rel_l2(getattr(got, f), getattr(want, f)) for f in ["vel", "stress", "temperature", "coord"]}
+    vel_tol = 1e-4 if name == "c1" else 1e-3      # EVP: see ONE_STEP
+    assert errs["vel"] <= vel_tol and errs["stress"] <= 1e-4 and errs["temperature"] <= 1e-8, errs
+
+
+@pytest.mark.gpu
+def test_fp32_trajectory_within_the_fp64_loops_own_sensitivity():
+    """Damping option 1: after 2,000 steps the FP32 form is no further from
+    the FP64 loop than the FP64 loop is from itself after a 1e-7 relative
+    change of the initial stress (about one FP32 rounding)."""
+    c = case("c1")
+    s0 = c.initial_state()
+    want = s0.copy()
+    c.oracle.step(want, 2000)
+    pert = s0.copy()
+    rng = np.random.default_rng(11)
+    pert.stress *= 1 + 1e-7 * rng.standard_normal(pert.stress.shape)
+    c.oracle.step(pert, 2000)
+    got, _ = run_fp32(c, s0, 2000)
+    for f in ["vel", "stress", "strain"]:
+        own = rel_l2(getattr(pert, f), getattr(want, f))
+        assert rel_l2(getattr(got, f), getattr(want, f)) <= 3 * own, (f, own)
+    assert rel_l2(got.temperature, want.temperature) <= 1e-8
+    assert rel_l2(got.coord, want.coord) <= 1e-6
+
+
+@pytest.mark.gpu
+def test_fp32_yielding_box_uses_the_fp64_return_map():
+    """Yielding elements go through the exact FP64 return map: from the same
+    state, one FP32 step stays within 1e-5 of the FP64 step and the same set of
+    elements yields."""
+    c = case("plastic")
+    s0 = c.state_after(30)
+    want = s0.copy()
+    c.oracle.step(want, 1)
+    got, rep = run_fp32(c, s0, 1)
+    assert rep.eigen_solves > 0
+    assert rel_l2(got.stress, want.stress) <= 1e-5
+    assert rel_l2(got.plstrain, want.plstrain) <= 1e-5
+    assert ((got.delta_plstrain > 0) != (want.delta_plstrain > 0)).sum() <= 2
