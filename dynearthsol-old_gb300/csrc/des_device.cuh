@@ -443,7 +443,7 @@ __device__ __forceinline__ bool surely_elastic(const double *s, double anphi, do
 }
 
 // returns 1 when the principal stresses were computed (+2 when QL was used,
-// +4 when QL failed to converge)
+// +4 when QL failed to converge, +16 for a shear return, +32 for a tensile one)
 __device__ __forceinline__ int elasto_plastic(double bulkm, double shearm, double amc, double anphi,
                                               double anpsi, double hardn, double ten_max,
                                               const double *de, double &depls, double *s)
@@ -465,12 +465,14 @@ __device__ __forceinline__ int elasto_plastic(double bulkm, double shearm, doubl
     double a2 = bulkm - 2. / 3 * shearm;
     double alam;
     if (h < 0) {
+        flags |= 16;
         alam = fs / (a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + 2 * sqrt(anphi) * hardn);
         p[0] -= alam * (a1 - a2 * anpsi);
         p[1] -= alam * (a2 - a2 * anpsi);
         p[2] -= alam * (a2 - a1 * anpsi);
         depls = fabs(alam) * sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18);
     } else {
+        flags |= 32;
         alam = ft / a1;
         p[0] -= alam * a2;
         p[1] -= alam * a2;

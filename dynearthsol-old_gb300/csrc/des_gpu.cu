@@ -11,7 +11,7 @@
 #include <vector>
 
 #include "des_gpu.h"
-#include "des_kernels32.cuh"
+#include "des_closure.cuh"
 
 using namespace des;
 
@@ -47,6 +47,8 @@ struct des_gpu {
     ConstsF *dF = nullptr;
     bool stress_bcs = false;
     int bfacets_count[DES_NBDRY] = {0};
+    MlpDev *dnet = nullptr;      // the learned closure (FP32 form), when set
+    bool closure = false;
 };
 
 namespace {
@@ -406,7 +408,12 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
         const DevF &f = g->f;
         kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f);
         if (ev) cudaEventRecord(ev[1], st);
-        kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
+        if (g->closure && g->hF.rheol == 7)
+            kf_fe_b_nn<7><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
+        else if (g->closure)
+            kf_fe_b_nn<5><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
+        else
+            kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
         if (ev) cudaEventRecord(ev[2], st);
         kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f);
         if (ev) cudaEventRecord(ev[3], st);
@@ -419,7 +426,10 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
         const Dev &d = g->d;
         k_fn_a<<<nb, kNodeBlock, 0, st>>>(d);
         if (ev) cudaEventRecord(ev[1], st);
-        k_fe_b<<<eb, kElemBlock, 0, st>>>(d);
+        if (d.ret_log)
+            k_fe_b_t<true><<<eb, kElemBlock, 0, st>>>(d);
+        else
+            k_fe_b_t<false><<<eb, kElemBlock, 0, st>>>(d);
         if (ev) cudaEventRecord(ev[2], st);
         k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d);
         if (ev) cudaEventRecord(ev[3], st);
@@ -479,7 +489,7 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     des_topology *topo = nullptr;
     rc = des_topology_build(m, &topo);
     if (rc) return rc;
-    des_gpu *g = new (std::nothrow) des_gpu;
+    des_gpu *g = new (std::nothrow) des_gpu();   // value-initialised: every device pointer starts null
     if (!g) {
         des_topology_free(topo);
         return DES_ERR_NOMEM;
@@ -666,7 +676,15 @@ int des_gpu_set_params(des_gpu *g, const des_params *p)
     if (p->precision != g->prec) return DES_ERR_ARG;   // the device layout depends on it
     g->P = *p;
     g->primed = false;
-    return build_consts(g);
+    rc = build_consts(g);
+    if (rc) return rc;
+    if (g->closure) {
+        // the stress pass with the closure is specialised on the rheology
+        if (g->graph) cudaGraphExecDestroy(g->graph);
+        g->graph = nullptr;
+        if (g->hF.rheol != 5 && g->hF.rheol != 7) g->closure = false;
+    }
+    return DES_OK;
 }
 
 long long des_gpu_device_bytes(const des_gpu *g) { return g ? g->bytes : 0; }
@@ -837,7 +855,90 @@ int des_gpu_report(des_gpu *g, des_step_report *r)
     r->status = c.status;
     r->ql_fallbacks = (long long)c.ql;
     r->eigen_solves = (long long)c.eig;
+    r->closure_candidates = (long long)c.nn_cand;
+    r->closure_accepted = (long long)c.nn_accept;
+    r->exact_returns = (long long)c.fp64_returns;
     return DES_OK;
+}
+
+int des_gpu_set_closure(des_gpu *g, const des_mlp *net)
+{
+    if (!g) return DES_ERR_ARG;
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+    if (!net) {
+        g->closure = false;
+        return DES_OK;
+    }
+    if (g->prec != DES_PREC_FP32 || (g->hF.rheol != 5 && g->hF.rheol != 7)) return DES_ERR_UNSUPPORTED;
+    // the network knows one material mix: its inputs carry no composition
+    if (g->hF.nmix != 1) return DES_ERR_UNSUPPORTED;
+    if (!(net->tol > 0.f) || !std::isfinite(net->tol)) return DES_ERR_ARG;
+    MlpDev h;
+    std::memset(&h, 0, sizeof(h));
+    for (int o = 0; o < kMlpHid; ++o)
+        for (int i = 0; i < kMlpIn; ++i) h.w1[o * kMlpIn + i] = __float2bfloat16(net->w1[o][i]);
+    for (int o = 0; o < kMlpHid; ++o)
+        for (int i = 0; i < kMlpHid; ++i) h.w2[o * kMlpHid + i] = __float2bfloat16(net->w2[o][i]);
+    for (int o = 0; o < kMlpOut; ++o)
+        for (int i = 0; i < kMlpHid; ++i)
+            h.w3[o * kMlpHid + i] = __float2bfloat16(o < kMlpOutUsed ? net->w3[o][i] : 0.f);
+    for (int i = 0; i < kMlpHid; ++i) {
+        h.b1[i] = net->b1[i];
+        h.b2[i] = net->b2[i];
+    }
+    for (int i = 0; i < kMlpOut; ++i) {
+        h.b3[i] = i < kMlpOutUsed ? net->b3[i] : 0.f;
+        h.out_scale[i] = net->out_scale[i];
+    }
+    for (int i = 0; i < kMlpIn; ++i) {
+        h.in_mean[i] = net->in_mean[i];
+        h.in_scale[i] = net->in_scale[i];
+        h.env_lo[i] = net->env_lo[i];
+        h.env_hi[i] = net->env_hi[i];
+    }
+    h.tol = net->tol;
+    if (!g->dnet) {
+        int rc = dev_alloc(g, &g->dnet, 1);
+        if (rc) return rc;
+    }
+    DES_CUDA(cudaMemcpyAsync(g->dnet, &h, sizeof(h), cudaMemcpyHostToDevice, g->stream));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    DES_CUDA(cudaFuncSetAttribute(kf_fe_b_nn<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(NnSmem)));
+    DES_CUDA(cudaFuncSetAttribute(kf_fe_b_nn<7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)sizeof(NnSmem)));
+    g->closure = true;
+    return DES_OK;
+}
+
+int des_gpu_log_returns(des_gpu *g, int nsteps, float *records, long long capacity, long long *count)
+{
+    if (!g || nsteps < 1 || capacity < 1 || !records || !count) return DES_ERR_ARG;
+    if (g->prec != DES_PREC_FP64 || g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (int rc = prime(g)) return rc;
+    float *buf = nullptr;
+    if (cudaMalloc(&buf, sizeof(float) * kRetRecord * (size_t)capacity) != cudaSuccess) return DES_ERR_NOMEM;
+    const unsigned long long zero = 0;
+    int rc = cuda_rc(cudaMemcpyAsync(&g->dclk->nlog, &zero, sizeof(zero), cudaMemcpyHostToDevice, g->stream));
+    if (!rc) {
+        g->d.ret_log = buf;
+        g->d.ret_cap = capacity;
+        for (int s = 0; s < nsteps; ++s) launch_step(g, nullptr);
+        g->d.ret_log = nullptr;
+        g->d.ret_cap = 0;
+        rc = finish(g);
+    }
+    Clock c;
+    if (!rc) rc = read_clock(g, c);
+    if (!rc) {
+        *count = (long long)c.nlog;
+        const long long n = std::min<long long>((long long)c.nlog, capacity);
+        if (n > 0)
+            rc = cuda_rc(cudaMemcpy(records, buf, sizeof(float) * kRetRecord * (size_t)n, cudaMemcpyDeviceToHost));
+    }
+    cudaFree(buf);
+    return rc;
 }
 
 int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)

@@ -38,6 +38,8 @@ struct Clock {
     unsigned long long minl, dtdiff;   // order_bits of running minima
     unsigned blocks_done, status;
     unsigned long long ql, eig;
+    unsigned long long nlog;                    // return-map records seen (logging launches)
+    unsigned long long nn_cand, nn_accept, fp64_returns;   // learned-closure counters
 };
 
 struct Dev {
@@ -56,6 +58,8 @@ struct Dev {
     double *c_mass, *c_tmass, *c_trdv;               // fused-pass contributions
     const Consts *K;
     Clock *clk;
+    float *ret_log;                  // return-map records (logging launches only)
+    long long ret_cap;
 };
 
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
@@ -183,6 +187,7 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
         double spII = second_invariant2(sp);
         if (svII < spII) {
             for (int i = 0; i < 6; ++i) s[i] = sv[i];
+            flags &= ~48;    // the plastic return was not taken
         } else {
             for (int i = 0; i < 6; ++i) s[i] = sp[i];
             pls += depls;
@@ -843,12 +848,22 @@ __global__ void k_fn_a(Dev d)
 }
 
 // E-B: edvoldt + update_stress + dp * volume
-__global__ void k_fe_b(Dev d)
+// One return-map record: the inputs and outputs of elasto_plastic for an
+// element that took the shear return (rheology.cxx:180-240 via :578-640).
+constexpr int kRetRecord = 24;
+// [0:6] stress before, [6:12] strain increment, [12] element temperature,
+// [13] plastic strain before, [14:20] stress after, [20] plastic-strain
+// increment, [21] element index (int bits), [22] step (int bits), [23] the
+// dilation factor anpsi of the return
+
+template <bool LOG>
+__global__ void k_fe_b_t(Dev d)
 {
     int e = gtid();
     if (e == 0) d.clk->mass_valid = 1;
     bool live = e < d.nelem;
     int flags = 0;
+    float rec[kRetRecord];
     if (live) {
         const size_t E = d.nelem;
         int4 c = d.conn[e];
@@ -863,7 +878,26 @@ __global__ void k_fe_b(Dev d)
         load6(d.strain, E, e, es);
         load6(d.srate_next, E, e, edot);
         double pls = d.pls[e], dpls = d.dpls[e], dpress;
+        const double pls_in = pls;
+        if (LOG)
+            for (int i = 0; i < 6; ++i) rec[i] = (float)s[i];
         flags = stress_body(d, e, c, edv, d.clk->dt, s, es, edot, pls, dpls, dpress);
+        if (LOG) {
+            double Tn[4];
+            load_nodal4(d.T, c, Tn);
+            for (int i = 0; i < 6; ++i) {
+                rec[6 + i] = (float)(edot[i] * d.clk->dt);
+                rec[14 + i] = (float)s[i];
+            }
+            double amc, anphi, anpsi, hardn, ten_max;
+            plastic_props(d.K->M, d.K->M.mix[d.mix[e]], pls_in, amc, anphi, anpsi, hardn, ten_max);
+            rec[12] = (float)elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]);
+            rec[13] = (float)pls_in;
+            rec[20] = (float)dpls;
+            rec[21] = __int_as_float(e);
+            rec[22] = __int_as_float(d.clk->steps);
+            rec[23] = (float)anpsi;
+        }
         store6(d.stress, E, e, s);
         store6(d.strain, E, e, es);
         store6(d.srate, E, e, edot);
@@ -873,6 +907,19 @@ __global__ void k_fe_b(Dev d)
         d.tmp_sg[e] = dpress * d.vol[e];
     }
     count_eigen(d, flags);
+    if (LOG) {
+        const bool w = live && (flags & 16);
+        const unsigned m = __ballot_sync(0xffffffffu, w);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&d.clk->nlog, (unsigned long long)__popc(m));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            const long long idx = (long long)base + __popc(m & ((1u << lane) - 1u));
+            if (w && idx < d.ret_cap)
+                for (int i = 0; i < kRetRecord; ++i) d.ret_log[idx * kRetRecord + i] = rec[i];
+        }
+    }
 }
 
 // E-C: NMD correction + element force vectors

@@ -10,6 +10,8 @@ import ctypes as C
 import os
 from pathlib import Path
 
+import numpy as np
+
 from . import abi
 from .abi import State, check
 from .build import LIB, build
@@ -68,6 +70,13 @@ def lib():
     L.des_abi_sizes.restype = None
     L.des_compute_dt_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                          P(abi.DtInputs), C.c_void_p, C.c_void_p]
+    fp = P(C.c_float)
+    L.des_mlp_forward.argtypes = [P(abi.Mlp), fp, C.c_longlong, fp]
+    L.des_mlp_loss_grad.argtypes = [P(abi.Mlp), fp, fp, C.c_longlong, P(C.c_double), P(abi.Mlp)]
+    L.des_mlp_train.argtypes = [P(abi.Mlp), fp, fp, C.c_longlong, C.c_int, C.c_int, C.c_float,
+                                C.c_ulonglong, fp]
+    L.des_gpu_log_returns.argtypes = [C.c_void_p, C.c_int, fp, C.c_longlong, P(C.c_longlong)]
+    L.des_gpu_set_closure.argtypes = [C.c_void_p, P(abi.Mlp)]
     _lib = L
     return L
 
@@ -186,6 +195,20 @@ class Device:
         return list(ms)
 
     @property
+    def log_returns(self, nsteps, capacity):
+        """Runs nsteps FP64 steps and returns the shear-return records
+        (float32 [n][24]) and how many returns there were in total."""
+        rec = np.zeros((capacity, abi.RET_RECORD), np.float32)
+        n = C.c_longlong()
+        _ck(lib().des_gpu_log_returns(self.h, nsteps, rec.ctypes.data_as(C.POINTER(C.c_float)),
+                                      capacity, C.byref(n)), "des_gpu_log_returns")
+        return rec[:min(n.value, capacity)], n.value
+
+    def set_closure(self, net):
+        """Installs an abi.Mlp as the learned closure (None removes it)."""
+        _ck(lib().des_gpu_set_closure(self.h, C.byref(net) if net is not None else None),
+            "des_gpu_set_closure")
+
     def kernels_per_step(self):
         return self.L.des_gpu_kernels_per_step(self.h)
 

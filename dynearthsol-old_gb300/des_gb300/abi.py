@@ -125,7 +125,28 @@ class Topology(C.Structure):
 class StepReport(C.Structure):
     _fields_ = [("steps", C.c_int), ("time", C.c_double), ("dt", C.c_double),
                 ("status", C.c_uint), ("ql_fallbacks", C.c_longlong),
-                ("eigen_solves", C.c_longlong)]
+                ("eigen_solves", C.c_longlong), ("closure_candidates", C.c_longlong),
+                ("closure_accepted", C.c_longlong), ("exact_returns", C.c_longlong)]
+
+
+MLP_IN, MLP_HID, MLP_OUT = 16, 64, 8
+RET_RECORD = 24      # floats per record of des_gpu_log_returns
+
+
+class Mlp(C.Structure):
+    """des_mlp: the learned closure's weights ([out][in]), normalisation,
+    training envelope and acceptance tolerance."""
+    _fields_ = [("w1", C.c_float * MLP_IN * MLP_HID), ("b1", C.c_float * MLP_HID),
+                ("w2", C.c_float * MLP_HID * MLP_HID), ("b2", C.c_float * MLP_HID),
+                ("w3", C.c_float * MLP_HID * MLP_OUT), ("b3", C.c_float * MLP_OUT),
+                ("in_mean", C.c_float * MLP_IN), ("in_scale", C.c_float * MLP_IN),
+                ("out_scale", C.c_float * MLP_OUT),
+                ("env_lo", C.c_float * MLP_IN), ("env_hi", C.c_float * MLP_IN),
+                ("tol", C.c_float)]
+
+    def arr(self, name):
+        """numpy view (float32) of one field."""
+        return np.ctypeslib.as_array(getattr(self, name))
 
 
 class DtInputs(C.Structure):

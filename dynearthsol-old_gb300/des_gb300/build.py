@@ -22,7 +22,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "--extended
               "-Xcompiler=-fPIC,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", f"-I{INCLUDE}"]
 
-CU_SOURCES = ["des_gpu.cu", "des_noalloc.cu"]
+CU_SOURCES = ["des_gpu.cu", "des_noalloc.cu", "des_mlp.cu"]
 CXX_SOURCES = ["topology.cpp", "workload.cpp"]
 
 

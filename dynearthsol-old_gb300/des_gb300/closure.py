@@ -1,0 +1,184 @@
+"""The learned return-map closure: training data, features and training.
+
+Records come from Device.log_returns, the FP64 form's own shear returns
+(rheology.cxx:180-240 reached from update_stress, :578-640).  Features and
+targets are formed here as the FP32 stress pass forms them on the device
+(csrc/des_closure.cuh); the network is trained on the GPU by des_mlp_train
+(csrc/des_mlp.cu) and installed with Device.set_closure.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+NIN, NOUT = 14, 7
+_FP = C.POINTER(C.c_float)
+
+
+def _lib():
+    from . import lib
+    return lib()
+
+
+def _ck(rc, what):
+    from . import _ck as ck
+    ck(rc, what)
+
+
+def _fptr(a):
+    assert a.dtype == np.float32 and a.flags.c_contiguous
+    return a.ctypes.data_as(_FP)
+
+
+def single_material(params):
+    """(bulk modulus, shear modulus, largest pls1) of a one-material model."""
+    if params.nmat != 1:
+        raise ValueError("the closure is trained for one material")
+    return (params.bulk_modulus.v[0], params.shear_modulus.v[0], params.pls1.v[0])
+
+
+def _dev(a):
+    d = a.copy()
+    d[:, :3] -= a[:, :3].mean(axis=1, keepdims=True)
+    return d
+
+
+def _j2(d):
+    return 0.5 * (d[:, :3] ** 2).sum(1) + (d[:, 3:] ** 2).sum(1)
+
+
+def trial_stress(rec, bulkm, shearm):
+    """Elastic trial s_old + C:de of each record (rheology.cxx:20-35)."""
+    s = rec[:, 0:6].astype(np.float64)
+    de = rec[:, 6:12].astype(np.float64)
+    lam = bulkm - 2.0 / 3.0 * shearm
+    t = s + 2.0 * shearm * de
+    t[:, :3] += (lam * de[:, :3].sum(1))[:, None]
+    return t
+
+
+def features(trial, T, pls, pls_sat):
+    """The 14 raw network inputs (padded to 16) and a mask of usable rows."""
+    d = _dev(trial)
+    j2 = _j2(d)
+    ok = j2 > 0
+    n = d / np.sqrt(np.where(ok, j2, 1.0))[:, None]
+    q = np.empty_like(n)
+    q[:, 0] = n[:, 0] ** 2 + n[:, 3] ** 2 + n[:, 4] ** 2
+    q[:, 1] = n[:, 3] ** 2 + n[:, 1] ** 2 + n[:, 5] ** 2
+    q[:, 2] = n[:, 4] ** 2 + n[:, 5] ** 2 + n[:, 2] ** 2
+    q[:, 3] = n[:, 0] * n[:, 3] + n[:, 3] * n[:, 1] + n[:, 4] * n[:, 5]
+    q[:, 4] = n[:, 0] * n[:, 4] + n[:, 3] * n[:, 5] + n[:, 4] * n[:, 2]
+    q[:, 5] = n[:, 3] * n[:, 4] + n[:, 1] * n[:, 5] + n[:, 5] * n[:, 2]
+    q = _dev(q)
+    raw = np.zeros((len(trial), abi.MLP_IN))
+    raw[:, 0:6] = n
+    raw[:, 6:12] = q
+    raw[:, 12] = T
+    raw[:, 13] = np.minimum(pls, pls_sat)
+    return raw, ok
+
+
+def targets(rec, trial, shearm):
+    """Network targets: the return per unit multiplier and depls/|alam|."""
+    depls = rec[:, 20].astype(np.float64)
+    anpsi = rec[:, 23].astype(np.float64)
+    c = np.sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18)
+    alam = -depls / c            # a shear return has fs < 0, so alam < 0
+    y = np.zeros((len(rec), abi.MLP_OUT))
+    y[:, 0:6] = (trial - rec[:, 14:20]) / (2.0 * shearm * alam)[:, None]
+    y[:, 6] = c
+    return y, depls > 0
+
+
+def dataset(rec, params):
+    """(raw inputs, targets) of the usable records."""
+    bulkm, shearm, pls_sat = single_material(params)
+    trial = trial_stress(rec, bulkm, shearm)
+    raw, ok1 = features(trial, rec[:, 12].astype(np.float64), rec[:, 13].astype(np.float64), pls_sat)
+    y, ok2 = targets(rec, trial, shearm)
+    ok = ok1 & ok2 & np.isfinite(y).all(1)
+    return raw[ok], y[ok]
+
+
+def new_net(seed, tol=1e-3):
+    """He-initialised network (zero padding rows and columns)."""
+    rng = np.random.default_rng(seed)
+    net = abi.Mlp()
+    w1 = net.arr("w1")
+    w1[:, :NIN] = rng.normal(0, np.sqrt(2.0 / NIN), (abi.MLP_HID, NIN))
+    net.arr("w2")[:] = rng.normal(0, np.sqrt(2.0 / abi.MLP_HID), (abi.MLP_HID, abi.MLP_HID))
+    net.arr("w3")[:NOUT] = rng.normal(0, np.sqrt(1.0 / abi.MLP_HID), (NOUT, abi.MLP_HID))
+    net.arr("in_scale")[:] = 1.0
+    net.arr("out_scale")[:] = 1.0
+    net.tol = tol
+    return net
+
+
+def fit_normalisation(net, raw, y, margin=0.02):
+    """Input mean/scale (directions stay as they are), output scales and the
+    training envelope of the normalised inputs, widened by `margin` of its
+    range."""
+    mean = np.zeros(abi.MLP_IN)
+    scale = np.ones(abi.MLP_IN)
+    for i in (12, 13):
+        mean[i] = raw[:, i].mean()
+        sd = raw[:, i].std()
+        scale[i] = 1.0 / sd if sd > 0 else 1.0
+    x = (raw - mean) * scale
+    lo, hi = x.min(0), x.max(0)
+    pad = margin * np.maximum(hi - lo, 1e-3)
+    osc = np.ones(abi.MLP_OUT)
+    osc[:NOUT] = np.maximum(np.abs(y[:, :NOUT]).std(0), 1e-6)
+    net.arr("in_mean")[:] = mean
+    net.arr("in_scale")[:] = scale
+    net.arr("env_lo")[:] = lo - pad
+    net.arr("env_hi")[:] = hi + pad
+    net.arr("out_scale")[:] = osc
+    return net
+
+
+def normalise(net, raw, y=None):
+    x = ((raw - net.arr("in_mean")) * net.arr("in_scale")).astype(np.float32)
+    x[:, NIN:] = 0
+    if y is None:
+        return np.ascontiguousarray(x)
+    t = (y / net.arr("out_scale")).astype(np.float32)
+    t[:, NOUT:] = 0
+    return np.ascontiguousarray(x), np.ascontiguousarray(t)
+
+
+def train(net, x, t, epochs=20, batch=1024, lr=2e-3, seed=1):
+    """Adam on the GPU over normalised (x, t); returns the mini-batch losses."""
+    n = len(x)
+    steps = max(1, int(epochs * n // batch))
+    trace = np.zeros(steps, np.float32)
+    _ck(_lib().des_mlp_train(C.byref(net), _fptr(x), _fptr(t), n, steps, batch, lr, seed,
+                             _fptr(trace)), "des_mlp_train")
+    return trace
+
+
+def forward(net, x):
+    """Network outputs (normalised) of normalised inputs, on the GPU."""
+    y = np.zeros((len(x), abi.MLP_OUT), np.float32)
+    _ck(_lib().des_mlp_forward(C.byref(net), _fptr(x), len(x), _fptr(y)), "des_mlp_forward")
+    return y
+
+
+def loss_grad(net, x, t):
+    """Loss and gradient (an abi.Mlp holding d loss / d weights) on the GPU."""
+    g = abi.Mlp()
+    loss = C.c_double()
+    _ck(_lib().des_mlp_loss_grad(C.byref(net), _fptr(x), _fptr(t), len(x), C.byref(loss),
+                                 C.byref(g)), "des_mlp_loss_grad")
+    return loss.value, g
+
+
+def fit(records, params, seed=1, epochs=20, batch=1024, lr=2e-3, tol=1e-3):
+    """Records -> trained closure (abi.Mlp) and the training losses."""
+    raw, y = dataset(records, params)
+    net = fit_normalisation(new_net(seed, tol), raw, y)
+    x, t = normalise(net, raw, y)
+    trace = train(net, x, t, epochs=epochs, batch=batch, lr=lr, seed=seed)
+    return net, trace

@@ -181,6 +181,9 @@ typedef struct des_step_report {
     unsigned  status;            /* DES_STATUS_* bits accumulated since create/upload */
     long long ql_fallbacks;      /* elements that took the QL branch of dsyevh3 */
     long long eigen_solves;      /* elements whose principal stresses were computed */
+    long long closure_candidates;   /* FP32 form with a closure: elements sent to the network */
+    long long closure_accepted;     /* ... whose prediction passed the checks */
+    long long exact_returns;        /* ... elements that took the exact FP64 return map */
 } des_step_report;
 
 typedef struct des_gpu des_gpu;
@@ -255,6 +258,63 @@ int  des_gpu_compute_shape_fn(des_gpu *g);     /* geometry.cxx:388-470 */
 int  des_gpu_update_mesh(des_gpu *g);          /* dynearthsol.cxx:237-261 */
 int  des_gpu_rotate_stress(des_gpu *g);        /* fields.cxx:455-533 */
 int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; also stores dt */
+
+/* ---- learned return-map closure (no reference counterpart) -------------- */
+/* A 14 -> 64 -> 64 -> 7 MLP with ReLU (inputs padded to 16, outputs to 8),
+ * BF16 weights and activations with FP32 accumulation on the tensor cores.
+ * It stands in for the Mohr-Coulomb return (rheology.cxx:180-240) of the
+ * FP32 form.  Inputs, functions of the element's old stress, strain
+ * increment, mean temperature and plastic strain: the direction n of the
+ * elastic trial's deviator (6), dev(n n) (6), T and the plastic strain
+ * (capped at the largest pls1), normalised as x = (raw - in_mean) *
+ * in_scale.  Outputs: (trial - new stress) / (2 G alam) (6) and the
+ * plastic-strain increment / |alam| (1), raw = y * out_scale, where alam is
+ * the plastic multiplier of the trial's FP32 principal stresses.  Weights
+ * are [out][in].  The des_mlp_* calls below take x and y already
+ * normalised. */
+#define DES_MLP_IN  16
+#define DES_MLP_HID 64
+#define DES_MLP_OUT 8
+typedef struct des_mlp {
+    float w1[DES_MLP_HID][DES_MLP_IN], b1[DES_MLP_HID];
+    float w2[DES_MLP_HID][DES_MLP_HID], b2[DES_MLP_HID];
+    float w3[DES_MLP_OUT][DES_MLP_HID], b3[DES_MLP_OUT];
+    float in_mean[DES_MLP_IN], in_scale[DES_MLP_IN];
+    float out_scale[DES_MLP_OUT];
+    float env_lo[DES_MLP_IN], env_hi[DES_MLP_IN];   /* training envelope of x */
+    float tol;                                      /* relative yield-residual tolerance */
+} des_mlp;
+
+/* y[n][8] = net(x[n][16]) on the tensor cores (host arrays). */
+int  des_mlp_forward(const des_mlp *net, const float *x, long long n, float *y);
+/* loss = mean over the n samples of the summed squared error of the 7
+ * outputs, and its gradient with respect to every weight and bias. */
+int  des_mlp_loss_grad(const des_mlp *net, const float *x, const float *y, long long n,
+                       double *loss, des_mlp *grad);
+/* Adam on the GPU for `steps` mini-batches of `batch` samples (shuffled once
+ * with `seed`), the step size decaying along a cosine from lr to lr / 100;
+ * net holds the initial and, on return, the trained weights.
+ * loss_trace[steps] (may be NULL) receives the mini-batch losses. */
+int  des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int steps,
+                   int batch, float lr, unsigned long long seed, float *loss_trace);
+
+/* Records the inputs and outputs of every shear return the FP64 form makes
+ * during nsteps steps (the training data of the closure; no reference
+ * counterpart).  Each record is 24 floats: stress before [6], strain
+ * increment [6], element temperature, plastic strain before, stress after
+ * [6], plastic-strain increment, element index and step (int bits), the
+ * dilation factor anpsi.  Up to `capacity` records are copied to `records`;
+ * *count receives how many there were.  FP64 form only. */
+int  des_gpu_log_returns(des_gpu *g, int nsteps, float *records, long long capacity,
+                         long long *count);
+
+/* Installs (net != NULL) or removes the learned closure in the FP32 form's
+ * stress pass: network candidates are judged by their yield residual at
+ * net->tol and fall back to the FP64 return map in the same kernel.  Needs
+ * the FP32 form, rh_ep or rh_evp and one material mix (DES_ERR_UNSUPPORTED
+ * otherwise).  The counts of candidates, accepted predictions and exact
+ * returns accumulate in des_step_report. */
+int  des_gpu_set_closure(des_gpu *g, const des_mlp *net);
 
 /* ---- stable dt without any device allocation ---------------------------- */
 /* Inputs of des_compute_dt_noalloc (the Param / MatProps values compute_dt

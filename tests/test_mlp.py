@@ -1,0 +1,132 @@
+"""CPU checks of the closure's gradient checker (oracle/mlp_ref.py) and of the
+host-side feature and target construction (des_gb300/closure.py)."""
+import numpy as np
+import pytest
+
+from des_gb300 import abi, closure
+from oracle import mlp_ref
+
+
+def _net(seed):
+    return mlp_ref.random_net(np.random.default_rng(seed))
+
+
+def _data(seed, n=96):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 16))
+    x[:, :14] = rng.normal(0, 1, (n, 14))
+    y = np.zeros((n, 8))
+    y[:, :7] = rng.normal(0, 1, (n, 7))
+    return x, y
+
+
+def test_bf16_rounding():
+    a = np.array([1.0, 1.00390625, 1.005859375, -3.14159, 0.0, 1e-3], np.float32)
+    r = mlp_ref.to_bf16(a)
+    # 1 + 2^-8 is halfway between 1 and 1 + 2^-7: ties to even gives 1
+    assert r[0] == 1.0 and r[1] == 1.0
+    assert r[2] == np.float32(1.0078125)
+    assert r[3] == np.float32(-3.140625)
+    assert r[4] == 0.0
+    assert abs(r[5] - 1e-3) / 1e-3 < 2 ** -8
+
+
+def test_fp64_gradient_matches_finite_differences():
+    net = _net(3)
+    x, y = _data(4)
+    loss, g = mlp_ref.loss_grad(net, x, y, bf16=False)
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    for name in ("w1", "b1", "w2", "b2", "w3", "b3"):
+        shape = net[name].shape
+        for _ in range(6):
+            idx = tuple(rng.integers(0, s) for s in shape)
+            if name == "w1" and idx[1] >= 14:
+                continue
+            if name in ("w3", "b3") and idx[0] >= 7:
+                continue
+            p = {k: v.copy() for k, v in net.items()}
+            p[name][idx] += h
+            lp, _ = mlp_ref.loss_grad(p, x, y, bf16=False)
+            p[name][idx] -= 2 * h
+            lm, _ = mlp_ref.loss_grad(p, x, y, bf16=False)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - g[name][idx]) <= 1e-6 * max(1.0, abs(fd)), (name, idx, fd, g[name][idx])
+
+
+def test_bf16_gradient_close_to_fp64():
+    """The BF16 operands move the gradient by about a percent; this bar is the
+    one the GPU kernels are held to against the FP64 formulas."""
+    net = _net(6)
+    x, y = _data(7, n=256)
+    _, g64 = mlp_ref.loss_grad(net, x, y, bf16=False)
+    _, g16 = mlp_ref.loss_grad(net, x, y, bf16=True)
+    for k in g64:
+        err = np.linalg.norm(g16[k] - g64[k]) / np.linalg.norm(g64[k])
+        assert err < 5e-2, (k, err)
+
+
+def _records(n, seed):
+    """Shear returns made by the oracle's restatement of elasto_plastic."""
+    import ctypes as C
+    from oracle.oracle import PortOracle
+    L = PortOracle.lib()
+    f = L.dso_elasto_plastic
+    dp = C.POINTER(C.c_double)
+    f.argtypes = [C.c_double] * 7 + [dp, dp, dp, C.POINTER(C.c_int)]
+    f.restype = None
+    rng = np.random.default_rng(seed)
+    K, G = 128e9, 30e9
+    recs = []
+    while len(recs) < n:
+        s = np.zeros(6)
+        s[:3] = -rng.uniform(1e7, 3e8) + rng.normal(0, 3e7, 3)
+        s[3:] = rng.normal(0, 2e7, 3)
+        de = rng.normal(0, 2e-4, 6)
+        phi = 30.0
+        sphi = np.sin(np.radians(phi))
+        anphi = (1 + sphi) / (1 - sphi)
+        anpsi = 1.0
+        amc = 2 * 4e6 * np.sqrt(anphi)
+        out = s.copy()
+        depls = C.c_double()
+        mode = C.c_int()
+        f(K, G, amc, anphi, anpsi, 0.0, 4e6 / np.tan(np.radians(phi)),
+          de.ctypes.data_as(dp), C.byref(depls), out.ctypes.data_as(dp), C.byref(mode))
+        if mode.value != 10:
+            continue
+        r = np.zeros(abi.RET_RECORD, np.float32)
+        r[0:6], r[6:12], r[12], r[13] = s, de, 500.0, 0.2
+        r[14:20], r[20], r[23] = out, depls.value, anpsi
+        recs.append(r)
+    return np.array(recs)
+
+
+def test_targets_reproduce_the_return():
+    """Rebuilding the new stress from the targets returns the oracle's own
+    output, and the return per multiplier is a function of the trial's
+    principal directions alone: with anpsi = 1 it is E_min - E_max, the
+    difference of the projectors on the least and most compressive axes."""
+    rec = _records(200, 11)
+    K, G = 128e9, 30e9
+    trial = closure.trial_stress(rec, K, G)
+    y, ok = closure.targets(rec, trial, G)
+    assert ok.all()
+    c = y[:, 6]
+    alam = -rec[:, 20].astype(np.float64) / c
+    rebuilt = trial - 2 * G * alam[:, None] * y[:, :6]
+    scale = np.abs(rec[:, 14:20]).max(1)
+    assert (np.abs(rebuilt - rec[:, 14:20]).max(1) / scale).max() < 1e-5
+    # the isotropic part of the return per multiplier is K (1 - anpsi) / G / 2 = 0 here
+    assert np.abs(y[:, :3].mean(1)).max() < 1e-4
+    M = np.zeros((len(trial), 3, 3))
+    for k, (i, j) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
+        M[:, i, j] = M[:, j, i] = trial[:, k]
+    _, V = np.linalg.eigh(M)
+    P = np.einsum("ni,nj->nij", V[:, :, 0], V[:, :, 0]) - np.einsum("ni,nj->nij", V[:, :, 2], V[:, :, 2])
+    Pv = np.stack([P[:, 0, 0], P[:, 1, 1], P[:, 2, 2], P[:, 0, 1], P[:, 0, 2], P[:, 1, 2]], 1)
+    assert np.abs(Pv - y[:, :6]).max() < 1e-4
+    raw, ok = closure.features(trial, rec[:, 12], rec[:, 13], 0.1)
+    assert ok.all()
+    assert np.allclose((raw[:, :6] ** 2)[:, :3].sum(1) * 0.5 + (raw[:, 3:6] ** 2).sum(1), 1.0)
+    assert raw[:, 13].max() == pytest.approx(0.1)
