@@ -194,7 +194,6 @@ class Device:
         _ck(self.L.des_gpu_profile_steps(self.h, nsteps, ms), "des_gpu_profile_steps")
         return list(ms)
 
-    @property
     def log_returns(self, nsteps, capacity):
         """Runs nsteps FP64 steps and returns the shear-return records
         (float32 [n][24]) and how many returns there were in total."""
@@ -209,6 +208,7 @@ class Device:
         _ck(lib().des_gpu_set_closure(self.h, C.byref(net) if net is not None else None),
             "des_gpu_set_closure")
 
+    @property
     def kernels_per_step(self):
         return self.L.des_gpu_kernels_per_step(self.h)
 

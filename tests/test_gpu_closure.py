@@ -1,0 +1,179 @@
+"""The learned return-map closure end to end: training data logged from the
+FP64 form's own returns (checked against the oracle), training on the GPU,
+and the FP32 stress pass with the network and its in-kernel FP64 fallback.
+
+The yielding box (low cohesion, friction and dilation weakening) is the
+workload: configs 1-3 do not yield within 2,000 steps, so the closure has
+nothing to replace there."""
+import numpy as np
+import pytest
+
+import des_gb300 as D
+from des_gb300 import abi, closure, workload as W
+from helpers import Case, LOOP, plastic_config, layered_config, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def fresh(cfg, prec, state=None):
+    mesh, p, T, pls, topo = D.setup_case(cfg)
+    p = abi.Params.from_buffer_copy(p)
+    p.precision = prec
+    dev = D.Device(mesh, p, device=0)
+    if state is None:
+        s = W.new_state(mesh, T, pls)
+        dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dev.init_fields()
+    else:
+        dev.upload(state, abi.F_ALL)
+    return dev, mesh, p
+
+
+def download(dev, mesh):
+    return dev.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+
+
+_trained = {}
+
+
+def trained(nx=12, ny=12, nz=6, nsteps=150):
+    """(config, records, FP64 state after nsteps, closure) of a yielding box."""
+    key = (nx, ny, nz, nsteps)
+    if key not in _trained:
+        cfg = plastic_config(nx, ny, nz)
+        d64, mesh, p = fresh(cfg, abi.PREC_FP64)
+        rec, n = d64.log_returns(nsteps, 2_000_000)
+        assert n == len(rec) and n > 0
+        s64 = download(d64, mesh)
+        d64.close()
+        net, trace = closure.fit(rec, p, epochs=15, seed=3)
+        assert np.isfinite(trace).all() and trace[-100:].mean() < 0.1 * trace[:100].mean()
+        _trained[key] = (cfg, rec, s64, net)
+    return _trained[key]
+
+
+def test_logged_returns_match_the_oracle():
+    """Every record is an oracle shear return at the same step and element,
+    with the same stress before, strain increment and outcome."""
+    cfg = plastic_config(8, 6, 4)
+    nsteps = 12
+    d64, mesh, p = fresh(cfg, abi.PREC_FP64)
+    rec, n = d64.log_returns(nsteps, 100_000)
+    d64.close()
+    assert n == len(rec) and n > 0
+    case = Case(cfg)
+    s = case.initial_state()
+    want = {}
+    for step in range(1, nsteps + 1):
+        s.steps += 1
+        s.time += s.dt
+        for f in LOOP:
+            if f == "update_temperature" and not case.params.has_thermal_diffusion:
+                continue
+            if f == "update_stress":
+                s_old, pls_old = s.stress.copy(), s.plstrain.copy()
+            case.oracle.call(f, s)
+            if f == "update_stress":
+                for e in np.nonzero(s.delta_plstrain > 0)[0]:
+                    want[(step, int(e))] = (s_old[e], pls_old[e], s.stress[e].copy(), s.delta_plstrain[e])
+        if s.steps % 10 == 0:
+            s.dt = case.oracle.call("compute_dt", s)
+    elem = rec[:, 21].view(np.int32)
+    step = rec[:, 22].view(np.int32)
+    assert len(set(zip(step.tolist(), elem.tolist()))) == len(rec)
+    for r, st, e in zip(rec, step, elem):
+        s_old, pls_old, s_new, depls = want[(int(st), int(e))]
+        sc = np.abs(s_old).max()
+        assert np.abs(r[0:6] - s_old).max() <= 1e-6 * sc
+        assert np.abs(r[14:20] - s_new).max() <= 1e-6 * sc
+        assert r[13] == pytest.approx(pls_old, rel=1e-6, abs=1e-12)
+        assert r[20] == pytest.approx(depls, rel=1e-5)
+        assert r[23] >= 1.0
+    # shear returns are most of the oracle's returns on this machine; the rest
+    # are tensile returns, which are not logged
+    assert len(rec) > 0.5 * len(want)
+
+
+def test_closure_rejecting_everything_is_the_exact_pass():
+    """With an empty training envelope every candidate falls back, and the
+    pass reproduces the FP32 form without a closure bit for bit."""
+    cfg, rec, s64, net = trained()
+    blank = abi.Mlp.from_buffer_copy(net)
+    blank.arr("env_lo")[:] = 1.0
+    blank.arr("env_hi")[:] = -1.0
+    a, mesh, _ = fresh(cfg, abi.PREC_FP32, s64)
+    a.set_closure(blank)
+    ra = a.step(5)
+    b, _, _ = fresh(cfg, abi.PREC_FP32, s64)
+    rb = b.step(5)
+    sa, sb = download(a, mesh), download(b, mesh)
+    a.close()
+    b.close()
+    assert ra.closure_candidates == 0 and ra.closure_accepted == 0
+    assert ra.exact_returns > 0 and ra.eigen_solves == rb.eigen_solves
+    for f in ("stress", "strain", "plstrain", "vel", "coord", "force"):
+        assert np.array_equal(getattr(sa, f), getattr(sb, f)), f
+
+
+def test_closure_accepts_and_stays_close_to_fp64():
+    """From the same FP64 state: one step with the closure against one FP64
+    step, and 150 steps from the start against the FP64 trajectory, each
+    compared with the FP32 form without the network."""
+    cfg, rec, s64, net = trained()
+    net = abi.Mlp.from_buffer_copy(net)
+    net.tol = 1e-3
+    # one step
+    d, mesh, _ = fresh(cfg, abi.PREC_FP64, s64)
+    d.step(1)
+    want = download(d, mesh)
+    d.close()
+    got = {}
+    reps = {}
+    for use in (False, True):
+        d, _, _ = fresh(cfg, abi.PREC_FP32, s64)
+        if use:
+            d.set_closure(net)
+        reps[use] = d.step(1)
+        got[use] = download(d, mesh)
+        d.close()
+    r = reps[True]
+    assert r.closure_candidates > 0
+    assert 0.1 * r.closure_candidates <= r.closure_accepted <= r.closure_candidates
+    assert r.exact_returns < reps[False].eigen_solves
+    e_nn = rel_l2(got[True].stress, want.stress)
+    e_32 = rel_l2(got[False].stress, want.stress)
+    assert e_32 < 1e-5
+    assert e_nn < 3 * net.tol, (e_nn, e_32)
+    assert rel_l2(got[True].plstrain, want.plstrain) < 3 * net.tol
+    # 150 steps from the start: the box is chaotic (damping option 1 and
+    # plasticity), so the bar is the FP32 form's own distance from FP64
+    errs = {}
+    for use in (False, True):
+        d, mesh, _ = fresh(cfg, abi.PREC_FP32)
+        if use:
+            d.set_closure(net)
+        d.step(150)
+        s = download(d, mesh)
+        d.close()
+        errs[use] = (rel_l2(s.stress, s64.stress), rel_l2(s.vel, s64.vel))
+    assert errs[True][0] <= 2 * errs[False][0] + 1e-3, errs
+    assert errs[True][1] <= 2 * errs[False][1] + 1e-3, errs
+
+
+def test_closure_needs_fp32_and_one_material():
+    cfg, rec, s64, net = trained()
+    d, _, _ = fresh(cfg, abi.PREC_FP64)
+    with pytest.raises(RuntimeError, match="error 5"):
+        d.set_closure(net)
+    d.close()
+    d, _, _ = fresh(layered_config(), abi.PREC_FP32)
+    with pytest.raises(RuntimeError, match="error 5"):
+        d.set_closure(net)
+    d.close()
+    bad = abi.Mlp.from_buffer_copy(net)
+    bad.tol = 0.0
+    d, _, _ = fresh(cfg, abi.PREC_FP32)
+    with pytest.raises(RuntimeError, match="error 2"):
+        d.set_closure(bad)
+    d.set_closure(None)
+    d.close()
