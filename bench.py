@@ -138,6 +138,97 @@ def cpu_baseline(cfg_key, steps=3, warmup=1):
                       f"{dt:.1f} s"}
 
 
+def _fresh_form(cfg, precision, local, params=None):
+    """A device with the initial state of cfg in the given precision."""
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+    mesh, p, T, pls, topo = D.setup_case(cfg)
+    q = abi.Params.from_buffer_copy(params if params is not None else p)
+    q.precision = precision
+    dv = D.Device(mesh, q, device=local)
+    s0 = W.new_state(mesh, T, pls)
+    dv.upload(s0, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+    dv.init_fields()
+    return dv, mesh, q
+
+
+def yielding_forms(args, local, world, barrier, reduce, compare):
+    """The three forms on the yielding workload, where the learned closure has
+    returns to replace: FP64 plain, FP32 mixed (exact FP64 returns) and FP32
+    with the closure.  The closure is trained first, on the GPU, from the
+    FP64 form's own returns on a small box of the same material."""
+    import des_gb300 as D
+    from des_gb300 import abi, closure, workload as W
+    base = W.CONFIGS["yield"]
+    cfg = base
+    if args.box:
+        nx, ny, nz = (int(v) for v in args.box.lower().split("x"))
+        cfg = W.scaled(base, nx, ny, nz)
+    t0 = time.perf_counter()
+    dv, tmesh, tp = _fresh_form(W.scaled(base, 24, 24, 8), abi.PREC_FP64, local)
+    rec, nrec = dv.log_returns(300, 4_000_000)
+    dv.close()
+    net, trace = closure.fit(rec, tp, epochs=20, seed=1)
+    net.tol = 1e-3
+    t_train = time.perf_counter() - t0
+    out = {"workload": f"{cfg.name}: weak Mohr-Coulomb material, about half the elements "
+                       "returning every step",
+           "closure_training": {"records": int(nrec), "box": f"24x24x8 x6 = {tmesh.nelem} tets, "
+                                "300 FP64 steps", "seconds": t_train,
+                                "loss_first": float(trace[:100].mean()),
+                                "loss_last": float(trace[-100:].mean()), "tol": net.tol}}
+    warm = max(args.warmup, 20)
+    prof = max(2, min(args.steps, 5))
+    names = ["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"]
+    d64 = S = None
+    for name, prec, use in (("fp64_plain", abi.PREC_FP64, False), ("fp32_mixed", abi.PREC_FP32, False),
+                            ("fp32_closure", abi.PREC_FP32, True)):
+        dv, mesh, _ = _fresh_form(cfg, prec, local)
+        if use:
+            dv.set_closure(net)
+        dv.step(warm)
+        r0 = dv.report()
+        barrier()
+        ms = dv.time_steps(args.steps)
+        barrier()
+        v, ms = replica_throughput(ms, mesh.nelem, args.steps, world, reduce)
+        r1 = dv.report()
+        passes = dv.profile_steps(prof)
+        k = args.steps
+        e = {"value": v, "ms_per_step": ms / k,
+             "passes_ms_per_step": {n: x / prof for n, x in zip(names, passes)},
+             "principal_stress_solves_per_step": (r1.eigen_solves - r0.eigen_solves) / k}
+        if use:
+            cand = r1.closure_candidates - r0.closure_candidates
+            acc = r1.closure_accepted - r0.closure_accepted
+            exact = r1.exact_returns - r0.exact_returns
+            e.update(network_candidates_per_step=cand / k, network_accepted_per_step=acc / k,
+                     exact_fp64_returns_per_step=exact / k,
+                     acceptance=acc / cand if cand else None,
+                     fallback_rate=(exact / (exact + acc)) if exact + acc else None)
+        if name == "fp64_plain":
+            d64 = dv
+            S = dv.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+            fp64_value = v
+        else:
+            errs = {}
+            for nsteps in (1, 100):
+                d64.upload(S, abi.F_ALL)
+                d64.step(nsteps)
+                a = d64.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+                dv.upload(S, abi.F_ALL)
+                dv.step(nsteps)
+                b = dv.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+                errs[f"after_{nsteps}_steps"] = compare(b, a)
+            e["rel_l2_vs_fp64_from_the_same_state"] = errs
+            e["speedup_vs_fp64"] = v / fp64_value
+            dv.close()
+        out[name] = e
+    d64.close()
+    out["fp32_closure"]["speedup_vs_fp32_mixed"] = out["fp32_closure"]["value"] / out["fp32_mixed"]["value"]
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -238,6 +329,10 @@ def run_ours(args):
                                        [t / prof32 for t in passes32])),
         "eigen_solves": rep32.eigen_solves, "clocks": clk32.summary()}
 
+    if not args.no_yielding:
+        forms["yielding"] = yielding_forms(args, local, world, barrier,
+                                           torch_reduce_max(f"cuda:{local}") if dist else None, compare)
+
     # per-pass device times over extra steps (same arithmetic, launched one by one)
     prof_steps = max(2, min(args.steps, 5))
     per_pass = dev.profile_steps(prof_steps)
@@ -326,6 +421,8 @@ def main():
     ap.add_argument("--config", default="2")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-yielding", action="store_true",
+                    help="skip the three forms on the yielding workload")
     ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
                     "(profiling of smaller cases)")
     args = ap.parse_args()

@@ -185,24 +185,26 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
             maxwell(xf.bulkm, xf.shearm, visc, dt, dv, de, sv);
         }
         float amc, anphi, anpsi, hardn, ten_max;
-        // the elastic bound exactly as the pass without a closure applies it
-        f_plastic_props(F, xf, (float)pls, amc, anphi, ten_max);
+        // the elastic tests exactly as the pass without a closure applies them
+        const float plsf = (float)pls, s0f = (float)s0;
+        f_plastic_props(F, xf, plsf, amc, anphi, ten_max);
         elastic(xf.bulkm, xf.shearm, de, s);
-        if (!f_surely_elastic(s, (float)s0, anphi, amc, ten_max)) {
+        float p[3];
+        if (!f_surely_elastic(s, s0f, anphi, amc, ten_max) &&
+            (f_principal_values(s, 0.f, p), !f_clearly_elastic(p, s0f, anphi, amc, ten_max))) {
             kind = 2;
-            f_plastic_full(F, xf, (float)pls, amc, anphi, anpsi, hardn, ten_max);
-            float p[3];
-            f_principal_values(s, 0.f, p);
-            const float s0f = (float)s0;
+            // FP32 throughout: the tests below have margins of tol S, and the
+            // FP32 sums are good to about 1e-7 S
+            f_plastic_full(F, xf, plsf, amc, anphi, anpsi, hardn, ten_max);
             cd.anphi = anphi;
             cd.hardn = hardn;
-            cd.cf = (float)((1.0 - (double)anphi) * s0 + (double)amc);
-            cd.ft_shift = (float)(s0 - (double)ten_max);
+            cd.cf = (1.f - anphi) * s0f + amc;
+            cd.ft_shift = s0f - ten_max;
             cd.S = fabsf(p[0] + s0f) + anphi * fabsf(p[2] + s0f) + amc;
             const float fs = p[0] - anphi * p[2] + cd.cf;
             const float pa = sqrtf(1.f + anphi * anphi) + anphi;
             const float ps = ten_max * anphi - amc;
-            const float h = p[2] + pa * p[0] + (float)(s0 - (double)ten_max + (double)pa * (s0 - (double)ps));
+            const float h = p[2] + s0f - ten_max + pa * (p[0] + s0f - ps);
             const float a1 = xf.bulkm + (4.f / 3.f) * xf.shearm, a2 = xf.bulkm - (2.f / 3.f) * xf.shearm;
             const float den = a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + 2.f * sqrtf(anphi) * hardn;
             cd.alam = fs / den;
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
             // so the network sees the plastic strain saturated there
             float pls_sat = 0.f;
             for (int m = 0; m < F.nmat; ++m) pls_sat = fmaxf(pls_sat, F.pls1[m]);
-            if (fs < -tol * cd.S && h < -tol * cd.S && nn_features(s, Te, fminf((float)pls, pls_sat), raw)) {
+            if (fs < -tol * cd.S && h < -tol * cd.S && nn_features(s, Te, fminf(plsf, pls_sat), raw)) {
                 bool inside = true;
                 for (int i = 0; i < kMlpInUsed; ++i) {
                     raw[i] = (raw[i] - net->in_mean[i]) * net->in_scale[i];

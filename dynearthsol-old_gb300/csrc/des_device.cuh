@@ -45,6 +45,10 @@ struct MatTable {
     // element's averaged angle equals it exactly)
     double phi_c, sphi_c, tphi_c, anphi_c, sqanphi_c;
     double psi_c, spsi_c, anpsi_c;
+    // the same for the fully weakened angles of material 0 (friction_angle1,
+    // dilation_angle1), which every element past pls1 uses
+    double phi_w, tphi_w, anphi_w, sqanphi_w;
+    double psi_w, anpsi_w;
     double visc_min, visc_max, tension_max;
     Mix    mix[kMaxMix];
 };
@@ -179,6 +183,10 @@ __device__ __forceinline__ void plastic_props(const MatTable &M, const Mix &x, d
         anphi = M.anphi_c;
         sqanphi = M.sqanphi_c;
         tphi = M.tphi_c;
+    } else if (phi == M.phi_w) {
+        anphi = M.anphi_w;
+        sqanphi = M.sqanphi_w;
+        tphi = M.tphi_w;
     } else {
         double sphi = sin(phi * kDeg2Rad);
         anphi = (1 + sphi) / (1 - sphi);
@@ -187,6 +195,8 @@ __device__ __forceinline__ void plastic_props(const MatTable &M, const Mix &x, d
     }
     if (psi == M.psi_c) {
         anpsi = M.anpsi_c;
+    } else if (psi == M.psi_w) {
+        anpsi = M.anpsi_w;
     } else {
         double spsi = sin(psi * kDeg2Rad);
         anpsi = (1 + spsi) / (1 - spsi);

@@ -165,6 +165,14 @@ int build_consts(des_gpu *g)
     double spsi = std::sin(M.psi_c * deg2rad);
     M.spsi_c = spsi;
     M.anpsi_c = (1 + spsi) / (1 - spsi);
+    M.phi_w = M.f1[0];
+    double sphi_w = std::sin(M.phi_w * deg2rad);
+    M.anphi_w = (1 + sphi_w) / (1 - sphi_w);
+    M.sqanphi_w = std::sqrt(M.anphi_w);
+    M.tphi_w = std::tan(M.phi_w * deg2rad);
+    M.psi_w = M.d1[0];
+    double spsi_w = std::sin(M.psi_w * deg2rad);
+    M.anpsi_w = (1 + spsi_w) / (1 - spsi_w);
     M.visc_min = p.visc_min;
     M.visc_max = p.visc_max;
     M.tension_max = p.tension_max;

@@ -207,6 +207,42 @@ __device__ __forceinline__ bool f_surely_elastic(const float *s, float s0, float
     return ((m - R) - anphi * (m + R) + amc) > margin && ((m + R) - ten_max) < -margin;
 }
 
+// FP32 principal values: eigenvalues of a symmetric 3x3 (xx yy zz xy xz yz) from the invariants of its
+// deviator (trigonometric form), ascending; the isotropic shift m is added
+// after, so a large pressure does not cancel the deviatoric part
+__device__ __forceinline__ void f_principal_values(const float *s, float shift, float p[3])
+{
+    float m = (s[0] + s[1] + s[2]) * (1.f / 3.f);
+    float a = s[0] - m, b = s[1] - m, c = s[2] - m;
+    float j2 = 0.5f * (a * a + b * b + c * c) + s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
+    float j3 = a * b * c + 2.f * s[3] * s[4] * s[5] - a * s[5] * s[5] - b * s[4] * s[4] - c * s[3] * s[3];
+    float r = sqrtf(j2 * (1.f / 3.f));
+    float cos3 = (r > 0.f) ? j3 / (2.f * r * r * r) : 0.f;
+    cos3 = fminf(fmaxf(cos3, -1.f), 1.f);
+    float th = acosf(cos3) * (1.f / 3.f);
+    float hi = 2.f * r * cosf(th), lo = 2.f * r * cosf(th + 2.0943951023931953f);
+    float mid = -(hi + lo);
+    p[0] = lo + m + shift;
+    p[1] = mid + m + shift;
+    p[2] = hi + m + shift;
+    if (p[1] < p[0]) { float tmp = p[0]; p[0] = p[1]; p[1] = tmp; }
+    if (p[2] < p[1]) { float tmp = p[1]; p[1] = p[2]; p[2] = tmp; }
+    if (p[1] < p[0]) { float tmp = p[0]; p[0] = p[1]; p[1] = tmp; }
+}
+
+// "No failure" (rheology.cxx:193, fs > 0 and ft < 0) from the FP32 principal
+// values of the trial (deviation form, plus s0), with a margin of 1e-2 of the
+// yield function's scale: the trigonometric eigenvalues are off by up to
+// about 2e-3 of the deviator's size next to a double eigenvalue, and the
+// FP32 sums by far less.
+__device__ __forceinline__ bool f_clearly_elastic(const float p[3], float s0f, float anphi, float amc,
+                                                  float ten_max)
+{
+    const float lo = p[0] + s0f, hi = p[2] + s0f;
+    const float margin = 1e-2f * (fabsf(lo) + anphi * fabsf(hi) + amc);
+    return lo - anphi * hi + amc > margin && hi - ten_max < -margin;
+}
+
 // the exact FP64 return map for one element (rheology.cxx:578-598), from the
 // FP32 state; returns eigen flags
 __device__ __noinline__ int ep_fp64(const Consts &K, const Mix &x, double pls, double s0,
@@ -236,6 +272,9 @@ __device__ __forceinline__ int f_elasto_plastic(const DevF &d, const MixF &xf, i
     elastic(xf.bulkm, xf.shearm, de, s_new);
     depls = 0;
     if (f_surely_elastic(s_new, (float)s0, anphi, amc, ten_max)) return 0;
+    float p[3];
+    f_principal_values(s_new, 0.f, p);
+    if (f_clearly_elastic(p, (float)s0, anphi, amc, ten_max)) return 0;
     const Consts &K = *d.K;
     return ep_fp64(K, K.M.mix[d.mix[e]], pls, s0, s_old, de, s_new, depls);
 }

@@ -155,28 +155,4 @@ __device__ __forceinline__ void mlp_forward16(const __nv_bfloat16 *X, const __nv
     __syncwarp();
 }
 
-// ---- principal values in FP32 for the acceptance test ----------------------
-// eigenvalues of a symmetric 3x3 (xx yy zz xy xz yz) from the invariants of its
-// deviator (trigonometric form), ascending; the isotropic shift m is added
-// after, so a large pressure does not cancel the deviatoric part
-__device__ __forceinline__ void f_principal_values(const float *s, float shift, float p[3])
-{
-    float m = (s[0] + s[1] + s[2]) * (1.f / 3.f);
-    float a = s[0] - m, b = s[1] - m, c = s[2] - m;
-    float j2 = 0.5f * (a * a + b * b + c * c) + s[3] * s[3] + s[4] * s[4] + s[5] * s[5];
-    float j3 = a * b * c + 2.f * s[3] * s[4] * s[5] - a * s[5] * s[5] - b * s[4] * s[4] - c * s[3] * s[3];
-    float r = sqrtf(j2 * (1.f / 3.f));
-    float cos3 = (r > 0.f) ? j3 / (2.f * r * r * r) : 0.f;
-    cos3 = fminf(fmaxf(cos3, -1.f), 1.f);
-    float th = acosf(cos3) * (1.f / 3.f);
-    float hi = 2.f * r * cosf(th), lo = 2.f * r * cosf(th + 2.0943951023931953f);
-    float mid = -(hi + lo);
-    p[0] = lo + m + shift;
-    p[1] = mid + m + shift;
-    p[2] = hi + m + shift;
-    if (p[1] < p[0]) { float tmp = p[0]; p[0] = p[1]; p[1] = tmp; }
-    if (p[2] < p[1]) { float tmp = p[1]; p[1] = p[2]; p[2] = tmp; }
-    if (p[1] < p[0]) { float tmp = p[0]; p[0] = p[1]; p[1] = tmp; }
-}
-
 }  // namespace des

@@ -7,6 +7,11 @@ Configs (sizes, physics, steps, seeds):
   4  config-2 mesh with config-3 rheology (the learned-closure case)
   5  400x400x80 x6      = 76,800,000 tets, 3 material layers
   "tiny" 4x3x2 x6 = 144 tets with the config-2 physics (golden fixtures)
+  "yield" the config-2 mesh with a weak elasto-plastic material (cohesion
+        4 -> 1 MPa, friction 30 -> 15 deg, dilation 0 -> 5 deg over plastic
+        strain 0 -> 0.01), inertial scaling 100 and visc_min 1e22: about half
+        the elements take a Mohr-Coulomb return every step, the workload of
+        the learned closure (configs 1-3 do not yield within 2,000 steps)
 
 Parameters not named by a config keep the reference defaults of input.cxx:15-456;
 the two defaults that would put quadratic host loops in the step
@@ -75,6 +80,10 @@ CONFIGS = {
                 t_bottom_c=1330.0, t_sigma=20.0, t_seed=20260205, nlayers=3,
                 layer_rho0=(2800.0, 3000.0, 3300.0), layer_depths=(0.3, 0.6), steps=1000),
     "tiny": Config("tiny_ep_4x3x2", 4, 3, 2, mesh_seed=7, weak_seed_row=True, steps=50),
+    "yield": Config("yield_ep_200x200x40", 200, 200, 40, mesh_seed=20260106, weak_seed_row=True,
+                    extra=dict(mats=dict(cohesion0=[4e6], cohesion1=[1e6], friction_angle1=[15.0],
+                                         dilation_angle1=[5.0], pls1=[0.01]),
+                               params=dict(inertial_scaling=100.0, visc_min=1e22))),
 }
 
 

@@ -74,20 +74,23 @@ def test_logged_returns_match_the_oracle():
                 s_old, pls_old = s.stress.copy(), s.plstrain.copy()
             case.oracle.call(f, s)
             if f == "update_stress":
+                # the two trajectories separate at about 1e-12 per step, so the
+                # comparison is against the state's own scales
+                sc, dsc = np.abs(s_old).max(), s.delta_plstrain.max()
                 for e in np.nonzero(s.delta_plstrain > 0)[0]:
-                    want[(step, int(e))] = (s_old[e], pls_old[e], s.stress[e].copy(), s.delta_plstrain[e])
+                    want[(step, int(e))] = (s_old[e], pls_old[e], s.stress[e].copy(), s.delta_plstrain[e],
+                                            sc, dsc)
         if s.steps % 10 == 0:
             s.dt = case.oracle.call("compute_dt", s)
     elem = rec[:, 21].view(np.int32)
     step = rec[:, 22].view(np.int32)
     assert len(set(zip(step.tolist(), elem.tolist()))) == len(rec)
     for r, st, e in zip(rec, step, elem):
-        s_old, pls_old, s_new, depls = want[(int(st), int(e))]
-        sc = np.abs(s_old).max()
+        s_old, pls_old, s_new, depls, sc, dsc = want[(int(st), int(e))]
         assert np.abs(r[0:6] - s_old).max() <= 1e-6 * sc
         assert np.abs(r[14:20] - s_new).max() <= 1e-6 * sc
-        assert r[13] == pytest.approx(pls_old, rel=1e-6, abs=1e-12)
-        assert r[20] == pytest.approx(depls, rel=1e-5)
+        assert r[13] == pytest.approx(pls_old, rel=1e-6, abs=1e-9)
+        assert r[20] == pytest.approx(depls, rel=1e-5, abs=1e-6 * dsc)
         assert r[23] >= 1.0
     # shear returns are most of the oracle's returns on this machine; the rest
     # are tensile returns, which are not logged
