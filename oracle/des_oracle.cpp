@@ -1312,4 +1312,11 @@ void dso_elasto_plastic(double bulkm, double shearm, double amc, double anphi, d
     elasto_plastic(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, *depls, s, *failure_mode);
 }
 
+void dso_plastic_props(const dso *o, int e, double pls, double out[7])
+{
+    out[0] = o->bulkm(e);
+    out[1] = o->shearm(e);
+    o->plastic_props(e, pls, out[2], out[3], out[4], out[5], out[6]);
+}
+
 }  // extern "C"

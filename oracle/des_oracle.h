@@ -61,6 +61,10 @@ void dso_principal_stresses3(const double s[6], double p[3], double v[9]);
 void dso_elasto_plastic(double bulkm, double shearm, double amc, double anphi, double anpsi,
                         double hardn, double ten_max, const double de[6], double *depls,
                         double s[6], int *failure_mode);
+/* element e's moduli and plastic properties at plastic strain pls
+ * (matprops.cxx:595-604, 687-704): out = bulkm, shearm, amc, anphi, anpsi,
+ * hardn, ten_max */
+void dso_plastic_props(const dso *o, int e, double pls, double out[7]);
 
 #ifdef __cplusplus
 }

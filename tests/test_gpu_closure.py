@@ -52,6 +52,25 @@ def trained(nx=12, ny=12, nz=6, nsteps=150):
     return _trained[key]
 
 
+def return_mode(case, e, s_old, de, pls):
+    """failure_mode of the oracle's elasto_plastic for one element (10 shear,
+    1 tensile, 0 none)."""
+    import ctypes as C
+    L = case.oracle.L
+    dp = C.POINTER(C.c_double)
+    L.dso_plastic_props.argtypes = [C.c_void_p, C.c_int, C.c_double, dp]
+    L.dso_plastic_props.restype = None
+    L.dso_elasto_plastic.argtypes = [C.c_double] * 7 + [dp, dp, dp, C.POINTER(C.c_int)]
+    L.dso_elasto_plastic.restype = None
+    pr = np.zeros(7)
+    L.dso_plastic_props(case.oracle.h, e, pls, pr.ctypes.data_as(dp))
+    s = np.ascontiguousarray(s_old, dtype=np.float64).copy()
+    d = np.ascontiguousarray(de, dtype=np.float64)
+    depls, mode = C.c_double(), C.c_int()
+    L.dso_elasto_plastic(*pr, d.ctypes.data_as(dp), C.byref(depls), s.ctypes.data_as(dp), C.byref(mode))
+    return mode.value
+
+
 def test_logged_returns_match_the_oracle():
     """Every record is an oracle shear return at the same step and element,
     with the same stress before, strain increment and outcome."""
@@ -72,6 +91,10 @@ def test_logged_returns_match_the_oracle():
                 continue
             if f == "update_stress":
                 s_old, pls_old = s.stress.copy(), s.plstrain.copy()
+                div = s.strain_rate[:, :3].sum(1)
+                de = s.strain_rate.copy()
+                de[:, :3] += ((s.edvoldt - div) / 3)[:, None]
+                de *= s.dt
             case.oracle.call(f, s)
             if f == "update_stress":
                 # the two trajectories separate at about 1e-12 per step, so the
@@ -79,22 +102,23 @@ def test_logged_returns_match_the_oracle():
                 sc, dsc = np.abs(s_old).max(), s.delta_plstrain.max()
                 for e in np.nonzero(s.delta_plstrain > 0)[0]:
                     want[(step, int(e))] = (s_old[e], pls_old[e], s.stress[e].copy(), s.delta_plstrain[e],
-                                            sc, dsc)
+                                            sc, dsc, return_mode(case, int(e), s_old[e], de[e], pls_old[e]))
         if s.steps % 10 == 0:
             s.dt = case.oracle.call("compute_dt", s)
     elem = rec[:, 21].view(np.int32)
     step = rec[:, 22].view(np.int32)
     assert len(set(zip(step.tolist(), elem.tolist()))) == len(rec)
     for r, st, e in zip(rec, step, elem):
-        s_old, pls_old, s_new, depls, sc, dsc = want[(int(st), int(e))]
+        s_old, pls_old, s_new, depls, sc, dsc, mode = want[(int(st), int(e))]
+        assert mode == 10
         assert np.abs(r[0:6] - s_old).max() <= 1e-6 * sc
         assert np.abs(r[14:20] - s_new).max() <= 1e-6 * sc
         assert r[13] == pytest.approx(pls_old, rel=1e-6, abs=1e-9)
         assert r[20] == pytest.approx(depls, rel=1e-5, abs=1e-6 * dsc)
         assert r[23] >= 1.0
-    # shear returns are most of the oracle's returns on this machine; the rest
-    # are tensile returns, which are not logged
-    assert len(rec) > 0.5 * len(want)
+    # and every shear return of the oracle was logged (tensile ones are not)
+    shear = [k for k, v in want.items() if v[-1] == 10]
+    assert len(shear) == len(rec)
 
 
 def test_closure_rejecting_everything_is_the_exact_pass():
