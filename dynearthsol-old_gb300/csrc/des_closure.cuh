@@ -51,7 +51,6 @@ struct NnSmem {
     float so[6][kNnBlock], de[6][kNnBlock];      // inputs of the exact return map
     float res[6][kNnBlock];                      // its outputs
     double resd[kNnBlock];
-    int resf[kNnBlock];
     int queue[kNnBlock];
     int wcount[kNnBlock / 32];
 };
@@ -146,8 +145,9 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
     const float tol = net->tol;
 
     int kind = 0;
-    float s[6], sv[6];       // trial (deviation form), Maxwell stress (rh_evp)
-    float visc = 0.f, dpls = 0.f;
+    float so[6], de[6];      // old stress and strain increment (deviation form)
+    float s[6], sv[6];       // trial, Maxwell stress (rh_evp)
+    float visc = 0.f, dpls = 0.f, dt = 0.f;
     double pls = 0.0, s0 = 0.0;
     NnCand cd = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     float raw[kMlpIn];
@@ -159,21 +159,19 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
         float edv = (d.ntmp[c.x] + d.ntmp[c.y] + d.ntmp[c.z] + d.ntmp[c.w]) * 0.25f;
         d.edvoldt[e] = edv;
         float es[6], edot[6];
-        f_load6(d.stress, E, e, s);
+        f_load6(d.stress, E, e, so);
         f_load6(d.strain, E, e, es);
         f_load6(d.srate_next, E, e, edot);
         pls = d.pls[e];
         s0 = d.s0[e];
         dpls = d.dpls[e];
-        const float dt = (float)d.clk->dt;
+        dt = (float)d.clk->dt;
         float div = tr3(edot);
         for (int i = 0; i < 3; ++i) edot[i] += (edv - div) * (1.f / 3.f);
-        float de[6];
         for (int i = 0; i < 6; ++i) {
             es[i] += edot[i] * dt;
             de[i] = edot[i] * dt;
-            S.so[i][tid] = s[i];
-            S.de[i][tid] = de[i];
+            s[i] = so[i];
         }
         f_store6(d.strain, E, e, es);
         f_store6(d.srate, E, e, edot);
@@ -181,7 +179,7 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
         if (RHEOL == 7) {
             visc = f_visc(F, xf, Te, edot);
             float dv = (float)(d.vol[e] / d.vol_old[e] - 1);
-            for (int i = 0; i < 6; ++i) sv[i] = s[i];
+            for (int i = 0; i < 6; ++i) sv[i] = so[i];
             maxwell(xf.bulkm, xf.shearm, visc, dt, dv, de, sv);
         }
         float amc, anphi, anpsi, hardn, ten_max;
@@ -220,112 +218,118 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                 }
                 if (inside) kind = 1;
             }
+            for (int i = 0; i < 6; ++i) {
+                S.so[i][tid] = so[i];
+                S.de[i][tid] = de[i];
+            }
         }
     }
 
-    // ---- compaction of the network candidates ----------------------------
-    const unsigned cmask = __ballot_sync(0xffffffffu, kind == 1);
-    if (lane == 0) S.wcount[w] = __popc(cmask);
-    __syncthreads();
-    int nc = 0, slot = 0;
-    for (int i = 0; i < kNnBlock / 32; ++i) {
-        if (i == w) slot = nc + __popc(cmask & ((1u << lane) - 1u));
-        nc += S.wcount[i];
-    }
-    if (kind == 1) {
-        __nv_bfloat16 *xr = S.x + slot * kMlpIn;
-        for (int i = 0; i < kMlpIn; i += 2)
-            *reinterpret_cast<uint32_t *>(xr + i) = pack_bf16(i < kMlpInUsed ? raw[i] : 0.f,
-                                                              i + 1 < kMlpInUsed ? raw[i + 1] : 0.f);
-    }
-    const int ntile = (nc + 15) >> 4;
-    if (tid >= nc && tid < ntile * 16)      // zero rows that pad the last tile
-        for (int i = 0; i < kMlpIn; i += 2) *reinterpret_cast<uint32_t *>(S.x + tid * kMlpIn + i) = 0u;
-    if (nc > 0) {
-        // the network's parameters, once per CTA that has candidates
-        const uint4 *src = reinterpret_cast<const uint4 *>(net->w1);
-        uint4 *dst = reinterpret_cast<uint4 *>(S.w1);
-        constexpr int nvec = (int)(sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3)) / 16;
-        for (int i = tid; i < nvec; i += kNnBlock) dst[i] = __ldg(src + i);
-        for (int i = tid; i < kMlpHid; i += kNnBlock) {
-            S.b1[i] = net->b1[i];
-            S.b2[i] = net->b2[i];
-        }
-        if (tid < kMlpOut) S.b3[tid] = net->b3[tid];
-    }
-    __syncthreads();
-    for (int t = w; t < ntile; t += kNnBlock / 32)
-        mlp_forward16(S.x + t * 16 * kMlpIn, S.w1, S.w2, S.w3, S.b1, S.b2, S.b3, S.h1[w], S.h2[w],
-                      S.y + t * 16 * kMlpOut);
-    __syncthreads();
-
-    // ---- judge the predictions -------------------------------------------
     float sp[6];
     double depls = 0.0;
-    if (kind == 1) {
-        const MixF &xf = F.mix[mixid];
-        const float *yo = S.y + slot * kMlpOut;
-        const float g2 = 2.f * xf.shearm * cd.alam;
-        for (int i = 0; i < 6; ++i) sp[i] = s[i] - g2 * yo[i] * net->out_scale[i];
-        const float dp = fabsf(cd.alam) * yo[6] * net->out_scale[6];
-        float p[3];
-        f_principal_values(sp, 0.f, p);
-        const float r = p[0] - cd.anphi * p[2] + cd.cf - 2.f * sqrtf(cd.anphi) * cd.hardn * cd.alam;
-        bool ok = dp > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
-        if (RHEOL == 7 && ok) {
-            // the Maxwell/plastic choice of rheology.cxx:628-638 must be clear
-            const float jv = second_invariant2(sv), jp = second_invariant2(sp);
-            ok = fabsf(jv - jp) > tol * fmaxf(jv, jp);
+    // CTAs whose elements are all elastic skip the network and the queue
+    if (__syncthreads_or(kind != 0)) {
+        // ---- compaction of the network candidates ------------------------
+        const unsigned cmask = __ballot_sync(0xffffffffu, kind == 1);
+        if (lane == 0) S.wcount[w] = __popc(cmask);
+        __syncthreads();
+        int nc = 0, slot = 0;
+        for (int i = 0; i < kNnBlock / 32; ++i) {
+            if (i == w) slot = nc + __popc(cmask & ((1u << lane) - 1u));
+            nc += S.wcount[i];
         }
-        if (ok)
-            depls = dp;
-        else
-            kind = 2;
-    }
-    const unsigned amask = __ballot_sync(0xffffffffu, kind == 1);
-    const unsigned xmask = __ballot_sync(0xffffffffu, kind == 2);
-    if (lane == 0) {
-        if (cmask) atomicAdd(&d.clk->nn_cand, (unsigned long long)__popc(cmask));
-        if (amask) atomicAdd(&d.clk->nn_accept, (unsigned long long)__popc(amask));
-        if (xmask) atomicAdd(&d.clk->fp64_returns, (unsigned long long)__popc(xmask));
-    }
+        if (kind == 1) {
+            __nv_bfloat16 *xr = S.x + slot * kMlpIn;
+            for (int i = 0; i < kMlpIn; i += 2)
+                *reinterpret_cast<uint32_t *>(xr + i) = pack_bf16(i < kMlpInUsed ? raw[i] : 0.f,
+                                                                  i + 1 < kMlpInUsed ? raw[i + 1] : 0.f);
+        }
+        const int ntile = (nc + 15) >> 4;
+        if (tid >= nc && tid < ntile * 16)      // zero rows that pad the last tile
+            for (int i = 0; i < kMlpIn; i += 2) *reinterpret_cast<uint32_t *>(S.x + tid * kMlpIn + i) = 0u;
+        if (nc > 0) {
+            // the network's parameters, once per CTA that has candidates
+            const uint4 *src = reinterpret_cast<const uint4 *>(net->w1);
+            uint4 *dst = reinterpret_cast<uint4 *>(S.w1);
+            constexpr int nvec = (int)(sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3)) / 16;
+            for (int i = tid; i < nvec; i += kNnBlock) dst[i] = __ldg(src + i);
+            for (int i = tid; i < kMlpHid; i += kNnBlock) {
+                S.b1[i] = net->b1[i];
+                S.b2[i] = net->b2[i];
+            }
+            if (tid < kMlpOut) S.b3[tid] = net->b3[tid];
+        }
+        __syncthreads();
+        for (int t = w; t < ntile; t += kNnBlock / 32)
+            mlp_forward16(S.x + t * 16 * kMlpIn, S.w1, S.w2, S.w3, S.b1, S.b2, S.b3, S.h1[w], S.h2[w],
+                          S.y + t * 16 * kMlpOut);
+        __syncthreads();
 
-    // ---- exact FP64 return map for the compacted rest ---------------------
-    __syncthreads();     // every warp has read its wcount entry above
-    if (lane == 0) S.wcount[w] = __popc(xmask);
-    __syncthreads();
-    int nx = 0, xslot = 0;
-    for (int i = 0; i < kNnBlock / 32; ++i) {
-        if (i == w) xslot = nx + __popc(xmask & ((1u << lane) - 1u));
-        nx += S.wcount[i];
-    }
-    if (kind == 2) S.queue[xslot] = tid;
-    __syncthreads();
-    int flags = 0;
-    if (tid < nx) {
-        const int j = S.queue[tid];
-        const int ej = blockIdx.x * kNnBlock + j;
-        float so[6], dej[6], out[6];
-        for (int i = 0; i < 6; ++i) {
-            so[i] = S.so[i][j];
-            dej[i] = S.de[i][j];
+        // ---- judge the predictions ---------------------------------------
+        if (kind == 1) {
+            const MixF &xf = F.mix[mixid];
+            const float *yo = S.y + slot * kMlpOut;
+            const float g2 = 2.f * xf.shearm * cd.alam;
+            for (int i = 0; i < 6; ++i) sp[i] = s[i] - g2 * yo[i] * net->out_scale[i];
+            const float dp = fabsf(cd.alam) * yo[6] * net->out_scale[6];
+            float p[3];
+            f_principal_values(sp, 0.f, p);
+            const float r = p[0] - cd.anphi * p[2] + cd.cf - 2.f * sqrtf(cd.anphi) * cd.hardn * cd.alam;
+            bool ok = dp > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
+            if (RHEOL == 7 && ok) {
+                // the Maxwell/plastic choice of rheology.cxx:628-638 must be clear
+                const float jv = second_invariant2(sv), jp = second_invariant2(sp);
+                ok = fabsf(jv - jp) > tol * fmaxf(jv, jp);
+            }
+            if (ok)
+                depls = dp;
+            else
+                kind = 2;
         }
-        const Consts &K = *d.K;
-        double dpj;
-        flags = ep_fp64(K, K.M.mix[d.mix[ej]], d.pls[ej], d.s0[ej], so, dej, out, dpj);
-        for (int i = 0; i < 6; ++i) S.res[i][j] = out[i];
-        S.resd[j] = dpj;
-        S.resf[j] = flags;
-    }
-    __syncthreads();
-    unsigned solved = __ballot_sync(0xffffffffu, flags & 1), ql = __ballot_sync(0xffffffffu, flags & 2);
-    if (lane == 0) {
-        if (solved) atomicAdd(&d.clk->eig, (unsigned long long)__popc(solved));
-        if (ql) atomicAdd(&d.clk->ql, (unsigned long long)__popc(ql));
+        const unsigned amask = __ballot_sync(0xffffffffu, kind == 1);
+        const unsigned xmask = __ballot_sync(0xffffffffu, kind == 2);
+        if (lane == 0) {
+            if (cmask) atomicAdd(&d.clk->nn_cand, (unsigned long long)__popc(cmask));
+            if (amask) atomicAdd(&d.clk->nn_accept, (unsigned long long)__popc(amask));
+            if (xmask) atomicAdd(&d.clk->fp64_returns, (unsigned long long)__popc(xmask));
+        }
+
+        // ---- exact FP64 return map for the compacted rest -----------------
+        __syncthreads();     // every warp has read its wcount entry above
+        if (lane == 0) S.wcount[w] = __popc(xmask);
+        __syncthreads();
+        int nx = 0, xslot = 0;
+        for (int i = 0; i < kNnBlock / 32; ++i) {
+            if (i == w) xslot = nx + __popc(xmask & ((1u << lane) - 1u));
+            nx += S.wcount[i];
+        }
+        if (kind == 2) S.queue[xslot] = tid;
+        __syncthreads();
+        int flags = 0;
+        if (tid < nx) {
+            const int j = S.queue[tid];
+            const int ej = blockIdx.x * kNnBlock + j;
+            float sj[6], dej[6], out[6];
+            for (int i = 0; i < 6; ++i) {
+                sj[i] = S.so[i][j];
+                dej[i] = S.de[i][j];
+            }
+            const Consts &K = *d.K;
+            double dpj;
+            flags = ep_fp64(K, K.M.mix[d.mix[ej]], d.pls[ej], d.s0[ej], sj, dej, out, dpj);
+            for (int i = 0; i < 6; ++i) S.res[i][j] = out[i];
+            S.resd[j] = dpj;
+        }
+        __syncthreads();
+        unsigned solved = __ballot_sync(0xffffffffu, flags & 1), ql = __ballot_sync(0xffffffffu, flags & 2);
+        if (lane == 0) {
+            if (solved) atomicAdd(&d.clk->eig, (unsigned long long)__popc(solved));
+            if (ql) atomicAdd(&d.clk->ql, (unsigned long long)__popc(ql));
+        }
     }
     if (!live) return;
 
-    // ---- results -----------------------------------------------------------
+    // ---- results -------------------------------------------------------------
     if (kind == 2) {
         for (int i = 0; i < 6; ++i) sp[i] = S.res[i][tid];
         depls = S.resd[tid];
@@ -333,26 +337,12 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
         depls = 0.0;
     }
-    const float old_s = S.so[0][tid] + S.so[1][tid] + S.so[2][tid];
     bool plastic = true;
     if (RHEOL == 7) {
-        if (kind == 2) {
-            float so[6], dej[6];
-            for (int i = 0; i < 6; ++i) {
-                so[i] = S.so[i][tid];
-                dej[i] = S.de[i][tid];
-            }
-            plastic = !f_viscous_wins(F.mix[mixid], so, dej, sv, sp, depls, (float)d.clk->dt, visc);
-        } else if (kind == 1) {
+        if (kind == 1)
             plastic = second_invariant2(sv) >= second_invariant2(sp);
-        } else {
-            float so[6], dej[6];
-            for (int i = 0; i < 6; ++i) {
-                so[i] = S.so[i][tid];
-                dej[i] = S.de[i][tid];
-            }
-            plastic = !f_viscous_wins(F.mix[mixid], so, dej, sv, sp, 0.0, (float)d.clk->dt, visc);
-        }
+        else
+            plastic = !f_viscous_wins(F.mix[mixid], so, de, sv, sp, depls, dt, visc);
     }
     if (plastic) {
         for (int i = 0; i < 6; ++i) s[i] = sp[i];
@@ -361,7 +351,7 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
     } else {
         for (int i = 0; i < 6; ++i) s[i] = sv[i];
     }
-    float dpv = tr3(s) - old_s;
+    float dpv = tr3(s) - tr3(so);
     f_store6(d.stress, E, e, s);
     d.pls[e] = pls;
     d.dpls[e] = dpls;

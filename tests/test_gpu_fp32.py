@@ -91,7 +91,11 @@ def test_fp32_one_step_from_the_same_state(name):
                 for f in ["vel", "force", "stress", "strain", "temperature", "coord"]}
         for f, tol in ONE_STEP[name].items():
             assert errs[f] <= tol, (k, errs)
-        assert errs["temperature"] <= 1e-12 and errs["coord"] <= 1e-12, (k, errs)
+        # coordinates are FP64 and move by v dt: they carry the velocity's
+        # error scaled by the step's displacement
+        shift = want.dt * np.linalg.norm(want.vel) / np.linalg.norm(want.coord)
+        assert errs["temperature"] <= 1e-12, (k, errs)
+        assert errs["coord"] <= 1e-13 + 1.01 * errs["vel"] * shift, (k, errs, shift)
 
 
 def smooth(cfg):
