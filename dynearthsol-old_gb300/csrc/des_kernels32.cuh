@@ -335,18 +335,46 @@ __device__ __forceinline__ void f_next_contrib(const DevF &d, int e, int4 c, con
     }
 }
 
-// FP64 part of the element force vectors for the next step: s0 grad(N_i) V,
-// plus rho_ref g V / 4 on z (fields.cxx:336-340 with the split stress)
-__device__ __forceinline__ void f_reference_force(const DevF &d, int e, const double gx[4],
-                                                  const double gy[4], const double gz[4], double vol)
+// FP64 geometry of the FP32 form: edge vectors from node 0, their cross
+// products c_i = 6 V grad(N_i) (the cofactors; c_0 = -(c_1 + c_2 + c_3)) and
+// the volume det / 6, the same quantities compute_volume (geometry.cxx:29-49)
+// and compute_shape_fn (geometry.cxx:388-470) form, grouped so that the
+// volume and the four gradients share one set of products.
+__device__ __forceinline__ double f_cofactors(const double X[4][3], double cf[4][3])
+{
+    double a[3], b[3], q[3];
+    for (int k = 0; k < 3; ++k) {
+        a[k] = X[1][k] - X[0][k];
+        b[k] = X[2][k] - X[0][k];
+        q[k] = X[3][k] - X[0][k];
+    }
+    // (fused multiply-adds: this form is held to a tolerance, not to the
+    // reference's rounding)
+    cf[1][0] = fma(b[1], q[2], -b[2] * q[1]);
+    cf[1][1] = fma(b[2], q[0], -b[0] * q[2]);
+    cf[1][2] = fma(b[0], q[1], -b[1] * q[0]);
+    cf[2][0] = fma(q[1], a[2], -q[2] * a[1]);
+    cf[2][1] = fma(q[2], a[0], -q[0] * a[2]);
+    cf[2][2] = fma(q[0], a[1], -q[1] * a[0]);
+    cf[3][0] = fma(a[1], b[2], -a[2] * b[1]);
+    cf[3][1] = fma(a[2], b[0], -a[0] * b[2]);
+    cf[3][2] = fma(a[0], b[1], -a[1] * b[0]);
+    for (int k = 0; k < 3; ++k) cf[0][k] = -(cf[1][k] + cf[2][k] + cf[3][k]);
+    return fma(a[0], cf[1][0], fma(a[1], cf[1][1], a[2] * cf[1][2]));     // 6 V
+}
+
+// FP64 part of the element force vectors for the next step: s0 grad(N_i) V
+// = s0 c_i / 6, plus rho_ref g V / 4 on z (fields.cxx:336-340 with the split
+// stress)
+__device__ __forceinline__ void f_reference_force(const DevF &d, int e, const double cf[4][3], double vol)
 {
     const size_t E = d.nelem;
-    const double s0 = d.s0[e];
-    const double buoy = d.F->gravity != 0.f ? d.F->mix[d.mix[e]].rho_ref * d.K->gravity / 4 : 0.0;
+    const double s6 = d.s0[e] * (1.0 / 6.0);
+    const double buoy = d.F->gravity != 0.f ? d.F->mix[d.mix[e]].rho_ref * d.K->gravity / 4 * vol : 0.0;
     for (int i = 0; i < 4; ++i) {
-        d.f0[(i)*E + e] = s0 * gx[i] * vol;
-        d.f0[(i + 4) * E + e] = s0 * gy[i] * vol;
-        d.f0[(i + 8) * E + e] = (s0 * gz[i] + buoy) * vol;
+        d.f0[(i)*E + e] = s6 * cf[i][0];
+        d.f0[(i + 4) * E + e] = s6 * cf[i][1];
+        d.f0[(i + 8) * E + e] = fma(s6, cf[i][2], buoy);
     }
 }
 
@@ -359,11 +387,10 @@ __global__ void kf_prime(DevF d)
     f_load_vel4(d, c, V);
     f_load_shp(d, e, dx, dy, dz);
     {
-        double X[4][3], gx[4], gy[4], gz[4];
+        double X[4][3], cf[4][3];
         f_load_xyz4(d, c, X);
-        double vol = d.vol[e];
-        shape_fn(X, vol, gx, gy, gz);
-        f_reference_force(d, e, gx, gy, gz, vol);
+        f_cofactors(X, cf);
+        f_reference_force(d, e, cf, d.vol[e]);
     }
     f_next_contrib(d, e, c, V, dx, dy, dz, (float)d.vol[e]);
 }
@@ -593,14 +620,16 @@ __device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, doubl
 {
     const size_t E = d.nelem;
     f_load_xyz4(d, c, X);
-    double vol = tet_volume(X[0], X[1], X[2], X[3]);
-    double gx[4], gy[4], gz[4];
-    shape_fn(X, vol, gx, gy, gz);
-    f_reference_force(d, e, gx, gy, gz, vol);
+    double cf[4][3];
+    const double det = f_cofactors(X, cf);
+    const double vol = det * (1.0 / 6.0);
+    f_reference_force(d, e, cf, vol);
+    // the gradients themselves are FP32: c_i / (6 V)
+    const float iv = 1.f / (float)det;
     for (int i = 0; i < 4; ++i) {
-        dx[i] = (float)gx[i];
-        dy[i] = (float)gy[i];
-        dz[i] = (float)gz[i];
+        dx[i] = (float)cf[i][0] * iv;
+        dy[i] = (float)cf[i][1] * iv;
+        dz[i] = (float)cf[i][2] * iv;
         d.shp[(0 + i) * E + e] = dx[i];
         d.shp[(4 + i) * E + e] = dy[i];
         d.shp[(8 + i) * E + e] = dz[i];

@@ -58,8 +58,11 @@ def test_fp32_init_matches_fp64():
     c = case("c1")
     want = c.initial_state()
     got, _ = run_fp32(c, None, 0, from_init=True)
-    assert got.dt == want.dt
-    for f in ["volume", "coord", "temperature", "plstrain"]:
+    # the FP32 form groups the FP64 volume and gradient products differently
+    # (one set of cofactors for both), so volume and dt agree to rounding
+    assert got.dt == pytest.approx(want.dt, rel=1e-14)
+    assert rel_l2(got.volume, want.volume) <= 1e-15
+    for f in ["coord", "temperature", "plstrain"]:
         assert np.array_equal(getattr(got, f), getattr(want, f)), f
     for f in ["stress", "strain", "mass", "tmass", "volume_n", "shpdx", "vel"]:
         assert rel_l2(getattr(got, f), getattr(want, f)) <= 1e-6, f
