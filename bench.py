@@ -171,8 +171,8 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     net, trace = closure.fit(rec, tp, epochs=20, seed=1)
     net.tol = 1e-3
     t_train = time.perf_counter() - t0
-    out = {"workload": f"{cfg.name}: weak Mohr-Coulomb material, about half the elements "
-                       "returning every step",
+    out = {"workload": f"{cfg.name}: weak Mohr-Coulomb material yielding from a weak-seed "
+                       "row (1-4% of the elements return each step over the timed steps)",
            "closure_training": {"records": int(nrec), "box": f"24x24x8 x6 = {tmesh.nelem} tets, "
                                 "300 FP64 steps", "seconds": t_train,
                                 "loss_first": float(trace[:100].mean()),
@@ -181,11 +181,14 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     prof = max(2, min(args.steps, 5))
     names = ["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"]
     d64 = S = None
-    for name, prec, use in (("fp64_plain", abi.PREC_FP64, False), ("fp32_mixed", abi.PREC_FP32, False),
-                            ("fp32_closure", abi.PREC_FP32, True)):
+    loose = abi.Mlp.from_buffer_copy(net)
+    loose.tol = 1e-2
+    for name, prec, use in (("fp64_plain", abi.PREC_FP64, None), ("fp32_mixed", abi.PREC_FP32, None),
+                            ("fp32_closure", abi.PREC_FP32, net),
+                            ("fp32_closure_tol_1e-2", abi.PREC_FP32, loose)):
         dv, mesh, _ = _fresh_form(cfg, prec, local)
-        if use:
-            dv.set_closure(net)
+        if use is not None:
+            dv.set_closure(use)
         dv.step(warm)
         r0 = dv.report()
         barrier()
@@ -198,7 +201,8 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
         e = {"value": v, "ms_per_step": ms / k,
              "passes_ms_per_step": {n: x / prof for n, x in zip(names, passes)},
              "principal_stress_solves_per_step": (r1.eigen_solves - r0.eigen_solves) / k}
-        if use:
+        if use is not None:
+            e["tol"] = use.tol
             cand = r1.closure_candidates - r0.closure_candidates
             acc = r1.closure_accepted - r0.closure_accepted
             exact = r1.exact_returns - r0.exact_returns
@@ -225,7 +229,8 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
             dv.close()
         out[name] = e
     d64.close()
-    out["fp32_closure"]["speedup_vs_fp32_mixed"] = out["fp32_closure"]["value"] / out["fp32_mixed"]["value"]
+    for k in ("fp32_closure", "fp32_closure_tol_1e-2"):
+        out[k]["speedup_vs_fp32_mixed"] = out[k]["value"] / out["fp32_mixed"]["value"]
     return out
 
 

@@ -9,9 +9,11 @@ Configs (sizes, physics, steps, seeds):
   "tiny" 4x3x2 x6 = 144 tets with the config-2 physics (golden fixtures)
   "yield" the config-2 mesh with a weak elasto-plastic material (cohesion
         4 -> 1 MPa, friction 30 -> 15 deg, dilation 0 -> 5 deg over plastic
-        strain 0 -> 0.01), inertial scaling 100 and visc_min 1e22: about half
-        the elements take a Mohr-Coulomb return every step, the workload of
-        the learned closure (configs 1-3 do not yield within 2,000 steps)
+        strain 0 -> 0.01), inertial scaling 100 and visc_min 1e22: yielding
+        spreads from the weak-seed row (1-4% of the elements return each step
+        over the first 100 steps at 200x200x40, about half of them on a
+        24x24x8 box), the workload of the learned closure (configs 1-3 do not
+        yield within 2,000 steps)
 
 Parameters not named by a config keep the reference defaults of input.cxx:15-456;
 the two defaults that would put quadratic host loops in the step
