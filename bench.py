@@ -152,6 +152,50 @@ def _fresh_form(cfg, precision, local, params=None):
     return dv, mesh, q
 
 
+def train_closure(base, local):
+    """The closure for base's material: 300 FP64 steps of a 24x24x8 box of it
+    logged, then 20 epochs of Adam on the GPU."""
+    from des_gb300 import abi, closure, workload as W
+    t0 = time.perf_counter()
+    dv, tmesh, tp = _fresh_form(W.scaled(base, 24, 24, 8), abi.PREC_FP64, local)
+    rec, nrec = dv.log_returns(300, 4_000_000)
+    dv.close()
+    net, trace = closure.fit(rec, tp, epochs=20, seed=1)
+    net.tol = 1e-3
+    info = {"records": int(nrec), "box": f"24x24x8 x6 = {tmesh.nelem} tets, 300 FP64 steps",
+            "seconds": time.perf_counter() - t0, "loss_first": float(trace[:100].mean()),
+            "loss_last": float(trace[-100:].mean()), "tol": net.tol}
+    return net, info
+
+
+def profile_form(args):
+    """One form alone (for ncu captures): warm-up, then the timed steps."""
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+    D.build()
+    base = W.CONFIGS[args.config]
+    cfg = base
+    if args.box:
+        nx, ny, nz = (int(v) for v in args.box.lower().split("x"))
+        cfg = W.scaled(base, nx, ny, nz)
+    net = None
+    if args.profile_form == "fp32_closure":
+        net, _ = train_closure(base, 0)
+    prec = abi.PREC_FP64 if args.profile_form == "fp64" else abi.PREC_FP32
+    dv, mesh, _ = _fresh_form(cfg, prec, 0)
+    if net is not None:
+        dv.set_closure(net)
+    dv.step(args.warmup)
+    ms = dv.time_steps(args.steps)
+    r = dv.report()
+    dv.close()
+    print(json.dumps({"profile_form": args.profile_form, "workload": cfg.name, "nelem": mesh.nelem,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                      "value": mesh.nelem * args.steps / (ms / 1e3), "unit": UNIT,
+                      "closure_candidates": r.closure_candidates, "closure_accepted": r.closure_accepted,
+                      "exact_returns": r.exact_returns}))
+
+
 def yielding_forms(args, local, world, barrier, reduce, compare):
     """The three forms on the yielding workload, where the learned closure has
     returns to replace: FP64 plain, FP32 mixed (exact FP64 returns) and FP32
@@ -164,19 +208,10 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     if args.box:
         nx, ny, nz = (int(v) for v in args.box.lower().split("x"))
         cfg = W.scaled(base, nx, ny, nz)
-    t0 = time.perf_counter()
-    dv, tmesh, tp = _fresh_form(W.scaled(base, 24, 24, 8), abi.PREC_FP64, local)
-    rec, nrec = dv.log_returns(300, 4_000_000)
-    dv.close()
-    net, trace = closure.fit(rec, tp, epochs=20, seed=1)
-    net.tol = 1e-3
-    t_train = time.perf_counter() - t0
+    net, training = train_closure(base, local)
     out = {"workload": f"{cfg.name}: weak Mohr-Coulomb material yielding from a weak-seed "
                        "row (1-4% of the elements return each step over the timed steps)",
-           "closure_training": {"records": int(nrec), "box": f"24x24x8 x6 = {tmesh.nelem} tets, "
-                                "300 FP64 steps", "seconds": t_train,
-                                "loss_first": float(trace[:100].mean()),
-                                "loss_last": float(trace[-100:].mean()), "tol": net.tol}}
+           "closure_training": training}
     warm = max(args.warmup, 20)
     prof = max(2, min(args.steps, 5))
     names = ["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"]
@@ -427,13 +462,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-yielding", action="store_true",
-                    help="skip the three forms on the yielding workload")
+                    help="skip the forms on the yielding workload")
+    ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure"], default=None,
+                    help="run one form alone on --config/--box (for profiling)")
     ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
                     "(profiling of smaller cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile_form:
+        profile_form(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)
