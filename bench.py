@@ -432,7 +432,11 @@ def run_ours(args):
                    "parallelism": f"replicas{world}", "l2": "state 4.8 GB >> 129 MB L2, no flush"},
         "gpu_launches": dev.kernels_per_step * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     # DRAM bytes per launch: 417 B/element read + written by E-A in the ncu
+                     # capture of profiles/k_fe_a_fp64_box100x100x40.md (traffic grows with the
+                     # element count), scaled to this launch
+                     "traffic": 417.0 * mesh.nelem if names[top] == "E-A" else None,
                      "peak_kind": hbm_kind,
                      "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm},
