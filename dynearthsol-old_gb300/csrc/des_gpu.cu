@@ -302,9 +302,28 @@ int build_consts(des_gpu *g)
 }
 
 // ---- host <-> device field transfers --------------------------------------
+// Page-locked host arrays (des_host_register, cudaHostAlloc) are reachable from
+// the GPU: on GB300 over NVLink-C2C.  The layout kernels then read or write the
+// host rows directly, one pass, without a staging copy; other host memory goes
+// through the staging buffer in chunks.
+const void *mapped(const void *host)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
 int upload_field(des_gpu *g, const double *host, double *dst, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
+    if (const double *m = static_cast<const double *>(mapped(host))) {
+        k_aos_to_soa<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(m, dst, ncomp, rows, 0, rows);
+        DES_LAUNCH();
+        return DES_OK;
+    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -319,6 +338,11 @@ int upload_field(des_gpu *g, const double *host, double *dst, int ncomp, long lo
 int download_field(des_gpu *g, double *host, const double *src, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
+    if (double *m = static_cast<double *>(const_cast<void *>(mapped(host)))) {
+        k_soa_to_aos<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(src, m, ncomp, rows, 0, rows);
+        DES_LAUNCH();
+        return DES_OK;
+    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -334,6 +358,11 @@ int download_field(des_gpu *g, double *host, const double *src, int ncomp, long 
 int upload_field(des_gpu *g, const double *host, float *dst, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
+    if (const double *m = static_cast<const double *>(mapped(host))) {
+        k_aos_to_soa_f<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(m, dst, ncomp, rows, 0, rows);
+        DES_LAUNCH();
+        return DES_OK;
+    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -348,6 +377,11 @@ int upload_field(des_gpu *g, const double *host, float *dst, int ncomp, long lon
 int download_field(des_gpu *g, double *host, const float *src, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
+    if (double *m = static_cast<double *>(const_cast<void *>(mapped(host)))) {
+        k_soa_to_aos_f<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(src, m, ncomp, rows, 0, rows);
+        DES_LAUNCH();
+        return DES_OK;
+    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -730,6 +764,11 @@ int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
     if (mask & DES_F_STRESS) {
         if (f32) {
             if (!h->stress) return DES_ERR_ARG;
+            if (const double *m = static_cast<const double *>(mapped(h->stress))) {
+                k_stress_split_tiled<<<blocks(E, 256), 256, 0, g->stream>>>(m, f.s0, f.stress, E);
+                DES_LAUNCH();
+                goto stress_done;
+            }
             long long chunk = std::max(1LL, g->staging_elems / 6);
             for (long long r0 = 0; r0 < E; r0 += chunk) {
                 long long nr = std::min(chunk, E - r0);
@@ -743,6 +782,7 @@ int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
             return rc;
         }
     }
+stress_done:
     UPX(DES_F_STRAIN, strain, strain, 0, 6, E)
     UPX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     UP(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
@@ -817,6 +857,11 @@ int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
     if (mask & DES_F_STRESS) {
         if (f32) {
             if (!h->stress) return DES_ERR_ARG;
+            if (double *m = static_cast<double *>(const_cast<void *>(mapped(h->stress)))) {
+                k_stress_join_tiled<<<blocks(E, 256), 256, 0, g->stream>>>(f.s0, f.stress, m, E);
+                DES_LAUNCH();
+                goto stress_down_done;
+            }
             long long chunk = std::max(1LL, g->staging_elems / 6);
             for (long long r0 = 0; r0 < E; r0 += chunk) {
                 long long nr = std::min(chunk, E - r0);
@@ -830,6 +875,7 @@ int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
             return rc;
         }
     }
+stress_down_done:
     DOWNX(DES_F_STRAIN, strain, strain, 0, 6, E)
     DOWNX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     DOWN(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)

@@ -785,6 +785,37 @@ __global__ void k_stress_join(const double *s0, const float *src, double *dst, l
     for (int c = 0; c < 6; ++c) dst[6 * r + c] = (double)src[c * ld + row0 + r] + (c < 3 ? m : 0.0);
 }
 
+// the same two layout changes for page-locked host rows read or written in
+// place: a block moves 256 rows through shared memory so that the host side
+// is touched in whole contiguous runs
+__global__ void k_stress_split_tiled(const double *src, double *s0, float *dst, long long rows)
+{
+    __shared__ double t[256 * 6];
+    const long long r0 = (long long)blockIdx.x * 256;
+    const int nr = (int)min(256LL, rows - r0);
+    for (int i = threadIdx.x; i < nr * 6; i += blockDim.x) t[i] = src[r0 * 6 + i];
+    __syncthreads();
+    const int r = threadIdx.x;
+    if (r >= nr) return;
+    const double *a = t + 6 * r;
+    double m = (a[0] + a[1] + a[2]) / 3;
+    s0[r0 + r] = m;
+    for (int c = 0; c < 6; ++c) dst[c * rows + r0 + r] = (float)(a[c] - (c < 3 ? m : 0.0));
+}
+__global__ void k_stress_join_tiled(const double *s0, const float *src, double *dst, long long rows)
+{
+    __shared__ double t[256 * 6];
+    const long long r0 = (long long)blockIdx.x * 256;
+    const int nr = (int)min(256LL, rows - r0);
+    const int r = threadIdx.x;
+    if (r < nr) {
+        double m = s0[r0 + r];
+        for (int c = 0; c < 6; ++c) t[6 * r + c] = (double)src[c * rows + r0 + r] + (c < 3 ? m : 0.0);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nr * 6; i += blockDim.x) dst[r0 * 6 + i] = t[i];
+}
+
 __global__ void k_vol_to_f(const double *vol, float *volf, long long n)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
