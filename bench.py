@@ -152,6 +152,33 @@ def _fresh_form(cfg, precision, local, params=None):
     return dv, mesh, q
 
 
+def e2e_rate(dev, mesh, steps, barrier, world):
+    """element-steps/s through des_gpu_step_host with page-locked host arrays
+    (the whole loop state up and down every step), and the bytes each way."""
+    import des_gb300 as D
+    from des_gb300 import abi
+    host = abi.State(mesh.nnode, mesh.nelem)
+    dev.download(host, abi.F_ALL)
+    D.pin(host)
+    mask = abi.F_STEP_STATE
+    nb = {abi.F_COORD: 24 * mesh.nnode, abi.F_VEL: 24 * mesh.nnode, abi.F_FORCE: 24 * mesh.nnode,
+          abi.F_TEMPERATURE: 8 * mesh.nnode, abi.F_MASS: 24 * mesh.nnode,
+          abi.F_NTMP: 8 * mesh.nnode, abi.F_VOLUME: 16 * mesh.nelem,
+          abi.F_STRESS: 48 * mesh.nelem, abi.F_STRAIN: 48 * mesh.nelem,
+          abi.F_STRAIN_RATE: 48 * mesh.nelem, abi.F_PLSTRAIN: 16 * mesh.nelem,
+          abi.F_DPRESSURE: 8 * mesh.nelem, abi.F_EDVOLDT: 8 * mesh.nelem,
+          abi.F_SHAPE: 96 * mesh.nelem, abi.F_SCALARS: 0}
+    io_bytes = sum(v for k, v in nb.items() if mask & k)
+    dev.step_host(host, 1, mask)                # warm-up of the host path
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dev.step_host(host, 1, mask)
+    e2e_s = time.perf_counter() - t0
+    D.unpin(host)
+    return world * mesh.nelem * steps / e2e_s, io_bytes
+
+
 def train_closure(base, local):
     """The closure for base's material: 300 FP64 steps of a 24x24x8 box of it
     logged, then 20 epochs of Adam on the GPU."""
@@ -360,6 +387,7 @@ def run_ours(args):
         dev32.step(nsteps)
         b = dev32.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
         errs[f"after_{nsteps}_steps"] = compare(b, a)
+    e2e32, _ = e2e_rate(dev32, mesh, max(1, min(args.steps, 5)), barrier, world)
     dev32.close()
     dev.upload(S, abi.F_ALL)
     forms["fp32_mixed"] = {
@@ -367,7 +395,8 @@ def run_ours(args):
         "rel_l2_vs_fp64_from_the_same_state": errs,
         "passes_ms_per_step": dict(zip(["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"],
                                        [t / prof32 for t in passes32])),
-        "eigen_solves": rep32.eigen_solves, "clocks": clk32.summary()}
+        "eigen_solves": rep32.eigen_solves, "clocks": clk32.summary(),
+        "e2e": {"value": e2e32, "unit": UNIT, "note": "same host-buffer path as the line's e2e"}}
 
     if not args.no_yielding:
         forms["yielding"] = yielding_forms(args, local, world, barrier,
@@ -395,29 +424,9 @@ def run_ours(args):
     step_alg = (B_ELEM + B_NODE * r) * mesh.nelem
     step_gbs = step_alg / (ms / args.steps / 1e3) / 1e9
 
-    # end to end through the drop-in entry point with pinned host buffers:
+    # end to end through the drop-in entry point with page-locked host buffers:
     # every step uploads the loop's state from the host and downloads it back
-    host = abi.State(mesh.nnode, mesh.nelem)
-    dev.download(host, abi.F_ALL)
-    D.pin(host)
-    mask = abi.F_STEP_STATE
-    nb = {abi.F_COORD: 24 * mesh.nnode, abi.F_VEL: 24 * mesh.nnode, abi.F_FORCE: 24 * mesh.nnode,
-          abi.F_TEMPERATURE: 8 * mesh.nnode, abi.F_MASS: 24 * mesh.nnode,
-          abi.F_NTMP: 8 * mesh.nnode, abi.F_VOLUME: 16 * mesh.nelem,
-          abi.F_STRESS: 48 * mesh.nelem, abi.F_STRAIN: 48 * mesh.nelem,
-          abi.F_STRAIN_RATE: 48 * mesh.nelem, abi.F_PLSTRAIN: 16 * mesh.nelem,
-          abi.F_DPRESSURE: 8 * mesh.nelem, abi.F_EDVOLDT: 8 * mesh.nelem,
-          abi.F_SHAPE: 96 * mesh.nelem, abi.F_SCALARS: 0}
-    io_bytes = sum(v for k, v in nb.items() if mask & k)
-    e2e_steps = max(1, min(args.steps, 5))
-    dev.step_host(host, 1, mask)                # warm-up of the host path
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        dev.step_host(host, 1, mask)
-    e2e_s = time.perf_counter() - t0
-    D.unpin(host)
-    e2e = world * mesh.nelem * e2e_steps / e2e_s
+    e2e, io_bytes = e2e_rate(dev, mesh, max(1, min(args.steps, 5)), barrier, world)
 
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
