@@ -303,9 +303,11 @@ int build_consts(des_gpu *g)
 
 // ---- host <-> device field transfers --------------------------------------
 // Page-locked host arrays (des_host_register, cudaHostAlloc) are reachable from
-// the GPU: on GB300 over NVLink-C2C.  The layout kernels then read or write the
-// host rows directly, one pass, without a staging copy; other host memory goes
-// through the staging buffer in chunks.
+// the GPU (on GB300 over NVLink-C2C): uploads read the host rows in place, in
+// one pass with the layout change (as fast as the copy engine, ~200 GB/s
+// here).  Downloads go through the staging buffer and the copy engine, which
+// writes host memory faster (~190 GB/s) than kernel stores (~150 GB/s); other
+// host memory goes through the staging buffer both ways.
 const void *mapped(const void *host)
 {
     cudaPointerAttributes a;
@@ -338,11 +340,6 @@ int upload_field(des_gpu *g, const double *host, double *dst, int ncomp, long lo
 int download_field(des_gpu *g, double *host, const double *src, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
-    if (double *m = static_cast<double *>(const_cast<void *>(mapped(host)))) {
-        k_soa_to_aos<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(src, m, ncomp, rows, 0, rows);
-        DES_LAUNCH();
-        return DES_OK;
-    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -377,11 +374,6 @@ int upload_field(des_gpu *g, const double *host, float *dst, int ncomp, long lon
 int download_field(des_gpu *g, double *host, const float *src, int ncomp, long long rows)
 {
     if (!host) return DES_ERR_ARG;
-    if (double *m = static_cast<double *>(const_cast<void *>(mapped(host)))) {
-        k_soa_to_aos_f<<<blocks(rows * ncomp, 256), 256, 0, g->stream>>>(src, m, ncomp, rows, 0, rows);
-        DES_LAUNCH();
-        return DES_OK;
-    }
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
@@ -857,11 +849,6 @@ int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
     if (mask & DES_F_STRESS) {
         if (f32) {
             if (!h->stress) return DES_ERR_ARG;
-            if (double *m = static_cast<double *>(const_cast<void *>(mapped(h->stress)))) {
-                k_stress_join_tiled<<<blocks(E, 256), 256, 0, g->stream>>>(f.s0, f.stress, m, E);
-                DES_LAUNCH();
-                goto stress_down_done;
-            }
             long long chunk = std::max(1LL, g->staging_elems / 6);
             for (long long r0 = 0; r0 < E; r0 += chunk) {
                 long long nr = std::min(chunk, E - r0);
@@ -875,7 +862,6 @@ int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
             return rc;
         }
     }
-stress_down_done:
     DOWNX(DES_F_STRAIN, strain, strain, 0, 6, E)
     DOWNX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     DOWN(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
@@ -1079,11 +1065,54 @@ void des_abi_sizes(long long out[5])
     out[4] = sizeof(des_step_report);
 }
 
+// fields the loop body overwrites before it reads them (update_force,
+// update_strain_rate, compute_edvoldt, update_stress, the scratch arrays):
+// des_gpu_step_host downloads but does not upload them
+constexpr unsigned kStepOutputs =
+    DES_F_FORCE | DES_F_NTMP | DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT | DES_F_TMP_RESULT;
+
+// volume, shape derivatives and nodal masses from the device's coordinates
+// and temperature, the values update_mesh (dynearthsol.cxx:237-261) leaves
+static int derive_geometry(des_gpu *g)
+{
+    const int eb = blocks(g->nelem, kElemBlock), nb = blocks(g->nnode, kNodeBlock);
+    cudaStream_t s = g->stream;
+    if (g->prec == DES_PREC_FP32) {
+        kf_derive_geometry<<<eb, kElemBlock, 0, s>>>(g->f);
+        kf_mass_flush<<<nb, kNodeBlock, 0, s>>>(g->f);
+    } else {
+        k_volume<<<eb, kElemBlock, 0, s>>>(g->d, 0);
+        k_shape<<<eb, kElemBlock, 0, s>>>(g->d);
+        k_mass_elem<<<eb, kElemBlock, 0, s>>>(g->d, g->d.T);
+        k_mass_node<<<nb, kNodeBlock, 0, s>>>(g->d);
+    }
+    DES_LAUNCH();
+    Clock c;
+    if (int rc = read_clock(g, c)) return rc;
+    k_clock_set<<<1, 32, 0, g->stream>>>(g->dclk, c.time, c.dt, c.steps, 1);
+    DES_LAUNCH();
+    g->primed = false;
+    return finish(g);
+}
+
 int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
                       des_step_report *report)
 {
-    int rc = des_gpu_upload(g, host, mask);
+    if (!g || !host) return DES_ERR_ARG;
+    unsigned up = mask & ~kStepOutputs;
+    // with coordinates and temperature in hand, volume, shape derivatives and
+    // masses are recomputed on the device rather than copied (1.0 GB fewer
+    // host-to-device bytes per step for 9.6M elements); volume_old is copied
+    const unsigned derived = DES_F_VOLUME | DES_F_SHAPE | DES_F_MASS;
+    const bool derive = (up & DES_F_COORD) && (up & DES_F_TEMPERATURE) && (up & derived) == derived;
+    if (derive) up &= ~derived;
+    int rc = des_gpu_upload(g, host, up);
     if (rc) return rc;
+    if (derive) {
+        if (host->nelem != g->nelem) return DES_ERR_ARG;
+        if ((rc = upload_field(g, host->volume_old, g->d.vol_old, 1, g->nelem))) return rc;
+        if ((rc = derive_geometry(g))) return rc;
+    }
     rc = des_gpu_step(g, nsteps, report);
     if (rc) return rc;
     return des_gpu_download(g, host, mask);

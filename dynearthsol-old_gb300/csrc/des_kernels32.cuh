@@ -734,6 +734,27 @@ __global__ void kf_init_geometry(DevF d)
     d.c_tmass[e] = F.thermal ? r0 * xf.cp * volf * 0.25f : 0.f;
 }
 
+// volume, shape derivatives and mass contributions from the current
+// coordinates and temperature, as E-A leaves them at the end of a step (the
+// host-buffer path derives them instead of uploading them)
+__global__ void kf_derive_geometry(DevF d)
+{
+    int e = gtid();
+    if (e >= d.nelem) return;
+    int4 c = d.conn[e];
+    double X[4][3];
+    float dx[4], dy[4], dz[4];
+    double vol = f_geometry(d, e, c, X, dx, dy, dz);
+    d.vol[e] = vol;
+    float volf = (float)vol;
+    d.c_vol[e] = volf;
+    const ConstsF &F = *d.F;
+    const MixF &xf = F.mix[d.mix[e]];
+    float rT = f_rho(F, xf, f_elem_T(d, c));
+    d.c_mass[e] = (F.is_qs ? xf.rho_qs : rT) * volf * 0.25f;
+    if (F.thermal) d.c_tmass[e] = rT * xf.cp * volf * 0.25f;
+}
+
 __global__ void kf_vbcs(DevF d)
 {
     int n = gtid();
@@ -785,9 +806,9 @@ __global__ void k_stress_join(const double *s0, const float *src, double *dst, l
     for (int c = 0; c < 6; ++c) dst[6 * r + c] = (double)src[c * ld + row0 + r] + (c < 3 ? m : 0.0);
 }
 
-// the same two layout changes for page-locked host rows read or written in
-// place: a block moves 256 rows through shared memory so that the host side
-// is touched in whole contiguous runs
+// the same split for page-locked host rows read in place: a block moves 256
+// rows through shared memory so that the host side is read in whole
+// contiguous runs
 __global__ void k_stress_split_tiled(const double *src, double *s0, float *dst, long long rows)
 {
     __shared__ double t[256 * 6];
@@ -801,19 +822,6 @@ __global__ void k_stress_split_tiled(const double *src, double *s0, float *dst, 
     double m = (a[0] + a[1] + a[2]) / 3;
     s0[r0 + r] = m;
     for (int c = 0; c < 6; ++c) dst[c * rows + r0 + r] = (float)(a[c] - (c < 3 ? m : 0.0));
-}
-__global__ void k_stress_join_tiled(const double *s0, const float *src, double *dst, long long rows)
-{
-    __shared__ double t[256 * 6];
-    const long long r0 = (long long)blockIdx.x * 256;
-    const int nr = (int)min(256LL, rows - r0);
-    const int r = threadIdx.x;
-    if (r < nr) {
-        double m = s0[r0 + r];
-        for (int c = 0; c < 6; ++c) t[6 * r + c] = (double)src[c * rows + r0 + r] + (c < 3 ? m : 0.0);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < nr * 6; i += blockDim.x) dst[r0 * 6 + i] = t[i];
 }
 
 __global__ void k_vol_to_f(const double *vol, float *volf, long long n)

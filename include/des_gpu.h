@@ -233,9 +233,16 @@ int  des_gpu_init_fields(des_gpu *g);
  * options) as one CUDA graph per step.  report may be NULL. */
 int  des_gpu_step(des_gpu *g, int nsteps, des_step_report *report);
 
-/* Drop-in form with host buffers: uploads `mask` fields of host, runs nsteps,
- * downloads the same fields back.  The host arrays stay authoritative, as in
- * the reference loop. */
+/* Drop-in form with host buffers: uploads the `mask` fields of host that the
+ * loop body reads, runs nsteps, downloads all `mask` fields back.  The host
+ * arrays stay authoritative, as in the reference loop.  Fields the loop body
+ * overwrites before reading them (force, ntmp, strain_rate, dpressure,
+ * edvoldt, tmp_result) are not uploaded; when coordinates, temperature,
+ * volume, shape derivatives and masses are all in mask, the last three are
+ * recomputed on the device from the uploaded coordinates and temperature
+ * (update_mesh's own arithmetic, so the values equal what the previous step
+ * left) and only volume_old is copied.  Page-locked host arrays
+ * (des_host_register) are read in place by the upload. */
 int  des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
                        des_step_report *report);
 
