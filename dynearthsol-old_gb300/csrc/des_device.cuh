@@ -538,6 +538,15 @@ __device__ __forceinline__ double tri_area(const double *a, const double *b, con
     return sqrt(d0 * d0 + d1 * d1 + d2 * d2) / 2;
 }
 
+// geometry.cxx:472-509 (3D): 216 sqrt(3) V^2 / (sum of the face areas)^3, 1
+// for the regular tetrahedron; nf = 216 sqrt(3) from the host's libm
+__device__ __forceinline__ double elem_quality(const double X[4][3], double vol, double nf)
+{
+    double area_sum = (tri_area(X[0], X[1], X[2]) + tri_area(X[0], X[1], X[3]) + tri_area(X[2], X[3], X[0]) +
+                       tri_area(X[2], X[3], X[1]));
+    return nf * vol * vol / (area_sum * area_sum * area_sum);
+}
+
 // geometry.cxx:410-452; X[v][d] are the four vertex coordinates
 __device__ __forceinline__ void shape_fn(const double X[4][3], double vol, double dx[4], double dy[4],
                                          double dz[4])

@@ -49,6 +49,7 @@ struct des_gpu {
     int bfacets_count[DES_NBDRY] = {0};
     MlpDev *dnet = nullptr;      // the learned closure (FP32 form), when set
     bool closure = false;
+    unsigned long long *qout = nullptr;   // mesh-quality reductions
 };
 
 namespace {
@@ -898,6 +899,95 @@ int des_gpu_report(des_gpu *g, des_step_report *r)
     r->closure_candidates = (long long)c.nn_cand;
     r->closure_accepted = (long long)c.nn_accept;
     r->exact_returns = (long long)c.fp64_returns;
+    return DES_OK;
+}
+
+// host inverse of order_bits
+static double from_bits(unsigned long long b)
+{
+    unsigned long long r = (b >> 63) ? (b & 0x7fffffffffffffffULL) : ~b;
+    double x;
+    std::memcpy(&x, &r, sizeof x);
+    return x;
+}
+
+// elem_quality of every element into the scratch array (and the reductions of
+// the remesh checks into g->qout); returns the scratch array
+static int run_quality(des_gpu *g, const des_remesh_check *c, double **q)
+{
+    if (int rc = begin_fn(g)) return rc;     // the scratch array holds state of the fused passes
+    if (!g->qout) {
+        int rc = dev_alloc(g, &g->qout, 4);
+        if (rc) return rc;
+    }
+    QualityArgs a;
+    const Dev &d = g->d;
+    a.nelem = g->nelem;
+    a.nnode = g->nnode;
+    a.conn = d.conn;
+    a.x = d.x;
+    a.y = d.y;
+    a.z = d.z;
+    a.vol = d.vol;
+    a.bcflag = d.bcflag;
+    a.nf = 216 * std::sqrt(3.0);                          // geometry.cxx:491
+    a.smallest_vol = c ? c->smallest_size * 0.118 * std::pow(c->resolution, 3) : 0.0;   // remeshing.cxx:83,1905
+    a.bottom = c ? -c->zlength : 0.0;
+    a.dist = c ? c->max_boundary_distortion * c->resolution : 0.0;
+    a.check_bottom = c && (c->remeshing_option == 1 || c->remeshing_option == 2 || c->remeshing_option == 11);
+    a.q = g->prec == DES_PREC_FP32 ? reinterpret_cast<double *>(g->f.tmp) : d.tmp;
+    a.out = g->qout;
+    DES_CUDA(cudaMemsetAsync(g->qout, 0xff, 4 * sizeof(unsigned long long), g->stream));
+    const int eb = blocks(g->nelem, kElemBlock), nb = blocks(g->nnode, kNodeBlock);
+    k_quality<<<eb, kElemBlock, 0, g->stream>>>(a);
+    k_quality_worst<<<eb, kElemBlock, 0, g->stream>>>(a);
+    if (a.check_bottom) k_bottom_distortion<<<nb, kNodeBlock, 0, g->stream>>>(a);
+    DES_LAUNCH();
+    *q = a.q;
+    return DES_OK;
+}
+
+int des_gpu_bad_mesh_quality(des_gpu *g, const des_remesh_check *c, int *code, int *index,
+                             double *worst_quality)
+{
+    if (!g || !c || !code || !index) return DES_ERR_ARG;
+    double *q;
+    if (int rc = run_quality(g, c, &q)) return rc;
+    unsigned long long out[4];
+    DES_CUDA(cudaMemcpyAsync(out, g->qout, sizeof out, cudaMemcpyDeviceToHost, g->stream));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    // worst_elem_quality (geometry.cxx:512-526) starts from q = 1, element 0
+    double qw = 1;
+    int worst = 0;
+    if (out[0] != ~0ull && from_bits(out[0]) < 1) {
+        qw = from_bits(out[0]);
+        worst = (int)out[1];
+    }
+    qw = std::pow(qw, 1.0 / 3);                             // remeshing.cxx:1946
+    if (worst_quality) *worst_quality = qw;
+    // remeshing.cxx:1905-1954: tiny elements, then the bottom, then distortion
+    if (out[2] != ~0ull) {
+        *code = 3;
+        *index = (int)out[2];
+    } else if (out[3] != ~0ull) {
+        *code = 2;
+        *index = (int)out[3];
+    } else if (qw < c->min_quality) {
+        *code = 1;
+        *index = worst;
+    } else {
+        *code = 0;
+    }
+    return DES_OK;
+}
+
+int des_gpu_elem_quality(des_gpu *g, double *quality)
+{
+    if (!g || !quality) return DES_ERR_ARG;
+    double *q;
+    if (int rc = run_quality(g, nullptr, &q)) return rc;
+    DES_CUDA(cudaMemcpyAsync(quality, q, sizeof(double) * g->nelem, cudaMemcpyDeviceToHost, g->stream));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
     return DES_OK;
 }
 

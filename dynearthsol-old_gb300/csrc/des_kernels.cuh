@@ -1063,6 +1063,87 @@ __global__ void k_soa_to_aos(const double *src, double *dst, int ncomp, long lon
     dst[i] = src[c * ld + row0 + r];
 }
 
+// ---- mesh-quality checks (the remesh trigger) --------------------------------
+// Arrays both forms keep in FP64.  out[0] = minimum quality (order bits),
+// out[1] = first element with that quality, out[2] = first element smaller
+// than smallest_vol, out[3] = first bottom node farther than dist from the
+// bottom (each ~0ull when there is none).
+struct QualityArgs {
+    int nelem, nnode;
+    const int4 *conn;
+    const double *x, *y, *z, *vol;
+    const unsigned *bcflag;
+    double nf, smallest_vol, bottom, dist;
+    int check_bottom;
+    double *q;                       // per-element quality (scratch, E doubles)
+    unsigned long long *out;
+};
+
+__device__ __forceinline__ unsigned long long warp_min64(unsigned long long v)
+{
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+// minimum over the block, one atomicMin by thread 0; every thread of the
+// block calls it (blockDim.x a multiple of 32, at most 1024)
+__device__ __forceinline__ void block_min_to(unsigned long long v, unsigned long long *dst)
+{
+    __shared__ unsigned long long part[32];
+    v = warp_min64(v);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long m = part[0];
+        for (int i = 1; i < (int)(blockDim.x >> 5); ++i) m = part[i] < m ? part[i] : m;
+        if (m != ~0ull) atomicMin(dst, m);
+    }
+    __syncthreads();     // part is reused by the next call
+}
+
+// elem_quality of every element, its minimum, and the first element below
+// smallest_vol (remeshing.cxx:1905-1914)
+__global__ void k_quality(QualityArgs a)
+{
+    const int e = gtid();
+    unsigned long long qb = ~0ull, tiny = ~0ull;
+    if (e < a.nelem) {
+        const int4 c = a.conn[e];
+        const int n[4] = {c.x, c.y, c.z, c.w};
+        double X[4][3];
+        for (int i = 0; i < 4; ++i) {
+            X[i][0] = __ldg(a.x + n[i]);
+            X[i][1] = __ldg(a.y + n[i]);
+            X[i][2] = __ldg(a.z + n[i]);
+        }
+        const double v = a.vol[e];
+        const double q = elem_quality(X, v, a.nf);
+        a.q[e] = q;
+        qb = order_bits(q);
+        if (v < a.smallest_vol) tiny = (unsigned long long)e;
+    }
+    block_min_to(qb, &a.out[0]);
+    block_min_to(tiny, &a.out[2]);
+}
+// the first element with the minimum quality (worst_elem_quality's strict <)
+__global__ void k_quality_worst(QualityArgs a)
+{
+    const int e = gtid();
+    unsigned long long w = ~0ull;
+    if (e < a.nelem && order_bits(a.q[e]) == a.out[0]) w = (unsigned long long)e;
+    block_min_to(w, &a.out[1]);
+}
+// the first bottom node too far from the bottom (remeshing.cxx:1917-1934)
+__global__ void k_bottom_distortion(QualityArgs a)
+{
+    const int n = gtid();
+    unsigned long long f = ~0ull;
+    if (n < a.nnode && (a.bcflag[n] & kBoundZ0) && fabs(a.z[n] - a.bottom) > a.dist) f = (unsigned long long)n;
+    block_min_to(f, &a.out[3]);
+}
+
 __global__ void k_clock_set(Clock *clk, double time, double dt, int steps, int mass_valid)
 {
     if (threadIdx.x == 0 && blockIdx.x == 0) {

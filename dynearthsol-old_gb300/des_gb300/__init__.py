@@ -77,6 +77,9 @@ def lib():
                                 C.c_ulonglong, fp]
     L.des_gpu_log_returns.argtypes = [C.c_void_p, C.c_int, fp, C.c_longlong, P(C.c_longlong)]
     L.des_gpu_set_closure.argtypes = [C.c_void_p, P(abi.Mlp)]
+    L.des_gpu_bad_mesh_quality.argtypes = [C.c_void_p, P(abi.RemeshCheck), P(C.c_int), P(C.c_int),
+                                           P(C.c_double)]
+    L.des_gpu_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
     _lib = L
     return L
 
@@ -202,6 +205,18 @@ class Device:
         _ck(lib().des_gpu_log_returns(self.h, nsteps, rec.ctypes.data_as(C.POINTER(C.c_float)),
                                       capacity, C.byref(n)), "des_gpu_log_returns")
         return rec[:min(n.value, capacity)], n.value
+
+    def bad_mesh_quality(self, check):
+        """(code, index, cube root of the worst quality) of bad_mesh_quality."""
+        code, index, q = C.c_int(), C.c_int(-1), C.c_double()
+        _ck(self.L.des_gpu_bad_mesh_quality(self.h, C.byref(check), C.byref(code), C.byref(index),
+                                            C.byref(q)), "des_gpu_bad_mesh_quality")
+        return code.value, index.value, q.value
+
+    def elem_quality(self):
+        q = np.zeros(self.mesh.nelem)
+        _ck(self.L.des_gpu_elem_quality(self.h, abi.dptr(q)), "des_gpu_elem_quality")
+        return q
 
     def set_closure(self, net):
         """Installs an abi.Mlp as the learned closure (None removes it)."""

@@ -129,6 +129,13 @@ class StepReport(C.Structure):
                 ("closure_accepted", C.c_longlong), ("exact_returns", C.c_longlong)]
 
 
+class RemeshCheck(C.Structure):
+    """des_remesh_check: the mesh.* parameters of bad_mesh_quality."""
+    _fields_ = [("smallest_size", C.c_double), ("resolution", C.c_double), ("zlength", C.c_double),
+                ("max_boundary_distortion", C.c_double), ("min_quality", C.c_double),
+                ("remeshing_option", C.c_int)]
+
+
 MLP_IN, MLP_HID, MLP_OUT = 16, 64, 8
 RET_RECORD = 24      # floats per record of des_gpu_log_returns
 

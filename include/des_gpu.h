@@ -305,6 +305,29 @@ int  des_mlp_loss_grad(const des_mlp *net, const float *x, const float *y, long 
 int  des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int steps,
                    int batch, float lr, unsigned long long seed, float *loss_trace);
 
+/* ---- remesh trigger: bad_mesh_quality on the device ------------------- */
+typedef struct des_remesh_check {
+    double smallest_size;            /* mesh.smallest_size */
+    double resolution;               /* mesh.resolution */
+    double zlength;                  /* mesh.zlength (the bottom is at -zlength) */
+    double max_boundary_distortion;  /* mesh.max_boundary_distortion */
+    double min_quality;              /* mesh.min_quality */
+    int    remeshing_option;         /* mesh.remeshing_option */
+} des_remesh_check;
+
+/* bad_mesh_quality (remeshing.cxx:1893-1960) on the device state, with the
+ * reference's order of checks: *code = 3 and *index = the first element
+ * smaller than smallest_size * 0.118 * resolution^3; else 2 and the first
+ * bottom node farther than max_boundary_distortion * resolution from the
+ * bottom (remeshing options 1, 2, 11 only); else 1 and the first worst
+ * element when the cube root of the worst elem_quality is below min_quality;
+ * else 0.  *worst_quality (may be NULL) receives that cube root. */
+int  des_gpu_bad_mesh_quality(des_gpu *g, const des_remesh_check *check, int *code, int *index,
+                              double *worst_quality);
+/* elem_quality (geometry.cxx:472-509) of every element into host
+ * quality[nelem] (the "mesh quality" field of output.cxx:150-152). */
+int  des_gpu_elem_quality(des_gpu *g, double *quality);
+
 /* Records the inputs and outputs of every shear return the FP64 form makes
  * during nsteps steps (the training data of the closure; no reference
  * counterpart).  Each record is 24 floats: stress before [6], strain

@@ -1312,6 +1312,62 @@ void dso_elasto_plastic(double bulkm, double shearm, double amc, double anphi, d
     elasto_plastic(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, de, *depls, s, *failure_mode);
 }
 
+// geometry.cxx:472-509 (3D)
+static double elem_quality(const double *coord, const int *conn, const double *volume, int e)
+{
+    const int *c = conn + 4 * (size_t)e;
+    const double *a = coord + 3 * (size_t)c[0], *b = coord + 3 * (size_t)c[1];
+    const double *cc = coord + 3 * (size_t)c[2], *d = coord + 3 * (size_t)c[3];
+    const double vol = volume[e];
+    const double nf = 216 * std::sqrt(3.0);
+    double area_sum = (tri_area(a, b, cc) + tri_area(a, b, d) + tri_area(cc, d, a) + tri_area(cc, d, b));
+    return nf * vol * vol / (area_sum * area_sum * area_sum);
+}
+
+void dso_elem_quality(const dso *o, const des_state_view *s, double *quality)
+{
+    for (int e = 0; e < o->nelem; ++e) quality[e] = elem_quality(s->coord, o->conn.data(), s->volume, e);
+}
+
+// remeshing.cxx:1893-1960 (3D: sizefactor 0.118, remeshing.cxx:83)
+void dso_bad_mesh_quality(const dso *o, const des_state_view *s, const des_remesh_check *c, int *code,
+                          int *index, double *worst_quality)
+{
+    const double smallest_vol = c->smallest_size * 0.118 * std::pow(c->resolution, 3);
+    // worst_elem_quality (geometry.cxx:512-526)
+    double q = 1;
+    int worst = 0;
+    for (int e = 0; e < o->nelem; ++e) {
+        double qe = elem_quality(s->coord, o->conn.data(), s->volume, e);
+        if (qe < q) {
+            q = qe;
+            worst = e;
+        }
+    }
+    q = std::pow(q, 1.0 / 3);
+    if (worst_quality) *worst_quality = q;
+    *code = 0;
+    for (int e = 0; e < o->nelem; ++e)
+        if (s->volume[e] < smallest_vol) {
+            *code = 3;
+            *index = e;
+            return;
+        }
+    if (c->remeshing_option == 1 || c->remeshing_option == 2 || c->remeshing_option == 11) {
+        const double bottom = -c->zlength, dist = c->max_boundary_distortion * c->resolution;
+        for (int i = 0; i < o->nnode; ++i)
+            if ((o->bcflag[i] & 16u) && std::fabs(s->coord[3 * (size_t)i + 2] - bottom) > dist) {
+                *code = 2;
+                *index = i;
+                return;
+            }
+    }
+    if (q < c->min_quality) {
+        *code = 1;
+        *index = worst;
+    }
+}
+
 void dso_plastic_props(const dso *o, int e, double pls, double out[7])
 {
     out[0] = o->bulkm(e);

@@ -61,6 +61,11 @@ void dso_principal_stresses3(const double s[6], double p[3], double v[9]);
 void dso_elasto_plastic(double bulkm, double shearm, double amc, double anphi, double anpsi,
                         double hardn, double ten_max, const double de[6], double *depls,
                         double s[6], int *failure_mode);
+/* elem_quality (geometry.cxx:472-509) of every element of the state */
+void dso_elem_quality(const dso *o, const des_state_view *s, double *quality);
+/* bad_mesh_quality (remeshing.cxx:1893-1960); see des_gpu_bad_mesh_quality */
+void dso_bad_mesh_quality(const dso *o, const des_state_view *s, const des_remesh_check *c, int *code,
+                          int *index, double *worst_quality);
 /* element e's moduli and plastic properties at plastic strain pls
  * (matprops.cxx:595-604, 687-704): out = bulkm, shearm, amc, anphi, anpsi,
  * hardn, ten_max */

@@ -78,6 +78,11 @@ class PortOracle(_Base):
             L.dso_init_fields.argtypes = [C.c_void_p, P(abi.StateView)]
             L.dso_step.argtypes = [C.c_void_p, P(abi.StateView), C.c_int]
             L.dso_compute_dt.argtypes = [C.c_void_p, P(abi.StateView), P(C.c_double)]
+            L.dso_elem_quality.argtypes = [C.c_void_p, P(abi.StateView), P(C.c_double)]
+            L.dso_elem_quality.restype = None
+            L.dso_bad_mesh_quality.argtypes = [C.c_void_p, P(abi.StateView), P(abi.RemeshCheck),
+                                               P(C.c_int), P(C.c_int), P(C.c_double)]
+            L.dso_bad_mesh_quality.restype = None
             for f in FUNCTIONS:
                 getattr(L, "dso_" + f).argtypes = [C.c_void_p, P(abi.StateView)]
             L.dso_bcflag.argtypes = [C.c_void_p, P(C.c_uint)]
@@ -143,6 +148,21 @@ class PortOracle(_Base):
         if rc:
             raise RuntimeError(f"dso_step failed {rc}")
 
+    def elem_quality(self, state):
+        """elem_quality of every element (geometry.cxx:472-509)."""
+        v = state.view()
+        q = np.zeros(state.volume.shape[0])
+        self.L.dso_elem_quality(self.h, C.byref(v), abi.dptr(q))
+        return q
+
+    def bad_mesh_quality(self, state, check):
+        """(code, index, cube root of the worst quality) of remeshing.cxx:1893-1960."""
+        v = state.view()
+        code, index, q = C.c_int(), C.c_int(-1), C.c_double()
+        self.L.dso_bad_mesh_quality(self.h, C.byref(v), C.byref(check), C.byref(code), C.byref(index),
+                                    C.byref(q))
+        return code.value, index.value, q.value
+
     def bcflag(self):
         a = np.zeros(self.mesh.nnode, np.uint32)
         self.L.dso_bcflag(self.h, abi.uptr(a))
@@ -203,6 +223,9 @@ class RefOracle(_Base):
             L.dsr_bfacets.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
             L.dsr_normals.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
             L.dsr_dsyevh3.argtypes = [P(C.c_double)] * 3
+            L.dsr_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
+            L.dsr_worst_elem_quality.argtypes = [C.c_void_p, P(C.c_int)]
+            L.dsr_worst_elem_quality.restype = C.c_double
             cls._L = L
         return cls._L
 
@@ -265,6 +288,16 @@ class RefOracle(_Base):
         a = np.zeros((n.value, 2), np.int32)
         self.L.dsr_bfacets(self.h, b, C.byref(n), abi.iptr(a))
         return a
+
+    def elem_quality(self, state):
+        """The reference's elem_quality of every element, and its
+        worst_elem_quality (value, index)."""
+        self._in(state)
+        q = np.zeros(state.volume.shape[0])
+        self.L.dsr_elem_quality(self.h, abi.dptr(q))
+        w = C.c_int()
+        qw = self.L.dsr_worst_elem_quality(self.h, C.byref(w))
+        return q, qw, w.value
 
     def normals(self):
         bn = np.zeros((10, 3))

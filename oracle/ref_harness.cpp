@@ -398,6 +398,18 @@ int dsr_dsyevh3(const double a[9], double q[9], double w[3])
     return rc;
 }
 
+// geometry.cxx:472-526 on the harness's current state
+int dsr_elem_quality(const dsr *h, double *quality)
+{
+    for (int e = 0; e < h->var.nelem; ++e)
+        quality[e] = elem_quality(*h->var.coord, *h->var.connectivity, *h->var.volume, e);
+    return 0;
+}
+double dsr_worst_elem_quality(const dsr *h, int *worst)
+{
+    return worst_elem_quality(*h->var.coord, *h->var.connectivity, *h->var.volume, *worst);
+}
+
 void dsr_destroy(dsr *h) { (void)h; /* the reference's arrays are never freed by its own code */ }
 
 }  // extern "C"

@@ -89,3 +89,15 @@ def test_eigen_solver_on_well_separated_spectra():
         _, q2, w2 = dsyevh3(a, "ref")
         assert np.abs(w1 - w2).max() <= 1e-9 * np.abs(w2).max()
         assert np.abs(np.sort(w1) - w).max() <= 1e-7 * np.abs(w).max()
+
+
+def test_elem_quality_and_worst_bit_exact():
+    """elem_quality and worst_elem_quality (geometry.cxx:472-526), the core of
+    the remesh trigger, on a deformed yielding state."""
+    c, r = both(plastic_config())
+    s = c.state_after(30)
+    q = c.oracle.elem_quality(s)
+    qr, qw, w = r.elem_quality(s)
+    assert np.array_equal(q, qr)
+    first = int(np.argmin(q)) if q.min() < 1 else 0
+    assert w == first and qw == min(1.0, q.min())
