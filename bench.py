@@ -427,6 +427,15 @@ def run_ours(args):
     step_alg = (B_ELEM + B_NODE * r) * mesh.nelem
     step_gbs = step_alg / (ms / args.steps / 1e3) / 1e9
 
+    # the remesh trigger (bad_mesh_quality on the device), timed on the same state
+    chk = abi.RemeshCheck(smallest_size=0.01, resolution=cfg.xlength / cfg.nx, zlength=cfg.zlength,
+                          max_boundary_distortion=0.25, min_quality=0.4, remeshing_option=1)
+    dev.bad_mesh_quality(chk)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        qcode = dev.bad_mesh_quality(chk)
+    remesh_ms = (time.perf_counter() - t0) / 3 * 1e3
+
     # end to end through the drop-in entry point with page-locked host buffers:
     # every step uploads the loop's state from the host and downloads it back
     e2e, h2d_bytes, d2h_bytes = e2e_rate(dev, mesh, max(1, min(args.steps, 5)), barrier, world)
@@ -454,6 +463,9 @@ def run_ours(args):
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm},
         "passes_ms_per_step": {n: t / prof_steps for n, t in zip(names, per_pass)},
         "forms": forms,
+        "remesh_check": {"ms_per_call": remesh_ms, "result": list(qcode),
+                         "what": "bad_mesh_quality on the device (elem_quality of every element, "
+                                 "tiny-element and bottom checks), host wall time incl. the read-back"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d_bytes,
                 "d2h_bytes_per_step": d2h_bytes},
         "clocks": clk.summary(),
