@@ -618,14 +618,21 @@ __device__ __forceinline__ void jaumann(R *s, R dt, R w3, R w4, R w5)
     for (int i = 0; i < 6; ++i) s[i] += dt * inc[i];
 }
 
-// fields.cxx:130-143: element conduction vector tr[i] = kv sum_j (gradNi.gradNj) T_j
+// fields.cxx:130-143: element conduction vector tr[i] = kv sum_j (gradNi.gradNj) T_j.
+// gradNi.gradNj and gradNj.gradNi round identically (the products commute and
+// are summed in the same order), so the 10 distinct dot products are formed once.
 __device__ __forceinline__ void conduction(const double *dx, const double *dy, const double *dz,
                                            const double Tn[4], double kv, double tr[4])
 {
+    double D[4][4];
+    for (int i = 0; i < 4; ++i)
+        for (int j = i; j < 4; ++j) {
+            D[i][j] = dx[i] * dx[j] + dy[i] * dy[j] + dz[i] * dz[j];
+            D[j][i] = D[i][j];
+        }
     for (int i = 0; i < 4; ++i) {
         double diffusion = 0.;
-        for (int j = 0; j < 4; ++j)
-            diffusion += (dx[i] * dx[j] + dy[i] * dy[j] + dz[i] * dz[j]) * Tn[j];
+        for (int j = 0; j < 4; ++j) diffusion += D[i][j] * Tn[j];
         tr[i] = diffusion * kv;
     }
 }
