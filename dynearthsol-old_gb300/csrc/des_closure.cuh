@@ -22,17 +22,18 @@
 // compacted onto the first threads of the CTA, which run the FP64 return
 // map, so that the FP64 work is not spread over every warp.
 //
-// Network input (14, normalised as x = (raw - in_mean) * in_scale), all
+// Network input (14, normalised as x = (raw - in_mean) * in_scale; 5 used),
 // functions of the old stress, the strain increment, T and plastic strain:
-//   n = dev(trial) / sqrt(J2(trial))      6  direction of the trial deviator
-//   dev(n n)                              6  its square (carries the Lode angle)
-//   element temperature, plastic strain   2  (the latter capped at the largest
-//                                            pls1, past which nothing softens)
-// Network output (7, raw = y * out_scale):
-//   (trial - new stress) / (2 G alam)     6  the return per unit multiplier
-//   plastic-strain increment / |alam|     1
-// where alam = fs / (a1 - a2 anpsi + a1 anphi anpsi - a2 anphi
-// + 2 sqrt(anphi) hardn) comes from the FP32 principal values of the trial.
+//   the principal values of the unit deviator n of the elastic trial   3
+//   element temperature, plastic strain capped at the largest pls1      2
+// Network output (7, raw = y * out_scale; 4 used): a, b D, c D and
+// depls / |alam|, where the return per unit plastic multiplier is
+//   R = (trial - new stress) / (2 G alam) = a I + b n + c dev(n n)
+// (an isotropic function of the trial, so three coefficients describe it,
+// Cayley-Hamilton) and D = (3 l_min^2 - 1)(3 l_max^2 - 1) clears the poles
+// b and c have where two principal values meet.  alam = fs / (a1 - a2 anpsi
+// + a1 anphi anpsi - a2 anphi + 2 sqrt(anphi) hardn) comes from the FP32
+// principal values of the trial.
 #pragma once
 
 #include "des_kernels32.cuh"
@@ -96,16 +97,21 @@ __device__ __forceinline__ void f_plastic_full(const ConstsF &F, const MixF &x, 
     ten_max = (phi == 0.f) ? F.tension_max : fminf(F.tension_max, cohesion / tanf(phi * (float)kDeg2Rad));
 }
 
-// the 14 raw inputs of the network from the trial deviation stress
-__device__ __forceinline__ bool nn_features(const float *st, float T, float pls, float raw[kMlpIn])
+// The unit deviator n of the trial (deviation form st), dev(n n), and the
+// eigenvalues of n from the trial's principal values p (ascending).
+__device__ __forceinline__ bool nn_basis(const float *st, const float p[3], float n[6], float q[6], float lam[3])
 {
     const float m = (st[0] + st[1] + st[2]) * (1.f / 3.f);
-    float n[6] = {st[0] - m, st[1] - m, st[2] - m, st[3], st[4], st[5]};
+    n[0] = st[0] - m;
+    n[1] = st[1] - m;
+    n[2] = st[2] - m;
+    n[3] = st[3];
+    n[4] = st[4];
+    n[5] = st[5];
     const float j2 = 0.5f * (n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) + n[3] * n[3] + n[4] * n[4] + n[5] * n[5];
     if (!(j2 > 0.f)) return false;
     const float inv = rsqrtf(j2);
     for (int i = 0; i < 6; ++i) n[i] *= inv;
-    float q[6];
     q[0] = n[0] * n[0] + n[3] * n[3] + n[4] * n[4];
     q[1] = n[3] * n[3] + n[1] * n[1] + n[5] * n[5];
     q[2] = n[4] * n[4] + n[5] * n[5] + n[2] * n[2];
@@ -113,15 +119,18 @@ __device__ __forceinline__ bool nn_features(const float *st, float T, float pls,
     q[4] = n[0] * n[4] + n[3] * n[5] + n[4] * n[2];
     q[5] = n[3] * n[4] + n[1] * n[5] + n[5] * n[2];
     const float mq = (q[0] + q[1] + q[2]) * (1.f / 3.f);
-    for (int i = 0; i < 3; ++i) q[i] -= mq;
-    for (int i = 0; i < 6; ++i) {
-        raw[i] = n[i];
-        raw[6 + i] = q[i];
+    for (int i = 0; i < 3; ++i) {
+        q[i] -= mq;
+        lam[i] = (p[i] - m) * inv;
     }
-    raw[12] = T;
-    raw[13] = pls;
-    raw[14] = raw[15] = 0.f;
     return true;
+}
+
+// (3 l_min^2 - 1)(3 l_max^2 - 1), zero where the least or the most compressive
+// principal direction is not unique: the poles of the return's coefficients
+__device__ __forceinline__ float nn_pole(const float lam[3])
+{
+    return (3.f * lam[0] * lam[0] - 1.f) * (3.f * lam[2] * lam[2] - 1.f);
 }
 
 // what a candidate needs to turn the network output into a stress and to
@@ -210,7 +219,14 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
             // so the network sees the plastic strain saturated there
             float pls_sat = 0.f;
             for (int m = 0; m < F.nmat; ++m) pls_sat = fmaxf(pls_sat, F.pls1[m]);
-            if (fs < -tol * cd.S && h < -tol * cd.S && nn_features(s, Te, fminf(plsf, pls_sat), raw)) {
+            float nb[6], qb[6], lam[3];
+            if (fs < -tol * cd.S && h < -tol * cd.S && nn_basis(s, p, nb, qb, lam)) {
+                raw[0] = lam[0];
+                raw[1] = lam[1];
+                raw[2] = lam[2];
+                raw[3] = Te;
+                raw[4] = fminf(plsf, pls_sat);
+                for (int i = 5; i < kMlpIn; ++i) raw[i] = 0.f;
                 bool inside = true;
                 for (int i = 0; i < kMlpInUsed; ++i) {
                     raw[i] = (raw[i] - net->in_mean[i]) * net->in_scale[i];
@@ -267,15 +283,23 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
 
         // ---- judge the predictions ---------------------------------------
         if (kind == 1) {
+            // R = a I + (b / D) n + (c / D) dev(n n), the return per unit
+            // multiplier; sigma = trial - 2 G alam R
             const MixF &xf = F.mix[mixid];
             const float *yo = S.y + slot * kMlpOut;
+            float nb[6], qb[6], lam[3], p[3];
+            f_principal_values(s, 0.f, p);
+            nn_basis(s, p, nb, qb, lam);
+            const float D = nn_pole(lam);
+            const float a = yo[0] * net->out_scale[0];
+            const float b = yo[1] * net->out_scale[1] / D, c = yo[2] * net->out_scale[2] / D;
             const float g2 = 2.f * xf.shearm * cd.alam;
-            for (int i = 0; i < 6; ++i) sp[i] = s[i] - g2 * yo[i] * net->out_scale[i];
-            const float dp = fabsf(cd.alam) * yo[6] * net->out_scale[6];
-            float p[3];
+            for (int i = 0; i < 6; ++i) sp[i] = s[i] - g2 * ((i < 3 ? a : 0.f) + b * nb[i] + c * qb[i]);
+            const float dp = fabsf(cd.alam) * yo[3] * net->out_scale[3];
             f_principal_values(sp, 0.f, p);
             const float r = p[0] - cd.anphi * p[2] + cd.cf - 2.f * sqrtf(cd.anphi) * cd.hardn * cd.alam;
-            bool ok = dp > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
+            bool ok = fabsf(D) > 1e-4f && dp > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
+            for (int i = 0; i < 6; ++i) ok = ok && isfinite(sp[i]);
             if (RHEOL == 7 && ok) {
                 // the Maxwell/plastic choice of rheology.cxx:628-638 must be clear
                 const float jv = second_invariant2(sv), jp = second_invariant2(sp);

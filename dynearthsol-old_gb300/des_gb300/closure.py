@@ -13,6 +13,7 @@ import numpy as np
 from . import abi
 
 NIN, NOUT = 14, 7
+USED_IN, USED_OUT = 5, 4     # inputs and outputs the closure uses (the rest are zero)
 _FP = C.POINTER(C.c_float)
 
 
@@ -58,38 +59,87 @@ def trial_stress(rec, bulkm, shearm):
     return t
 
 
-def features(trial, T, pls, pls_sat):
-    """The 14 raw network inputs (padded to 16) and a mask of usable rows."""
+def _mat(a):
+    M = np.zeros((len(a), 3, 3))
+    for k, (i, j) in enumerate(((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))):
+        M[:, i, j] = M[:, j, i] = a[:, k]
+    return M
+
+
+def _inner(a, b):
+    """Frobenius inner product of symmetric tensors in (xx yy zz xy xz yz)."""
+    return (a[:, :3] * b[:, :3]).sum(1) + 2 * (a[:, 3:] * b[:, 3:]).sum(1)
+
+
+def basis(trial):
+    """The unit deviator n of each trial, dev(n n), the eigenvalues of n
+    (ascending) and a mask of rows with a nonzero deviator."""
     d = _dev(trial)
     j2 = _j2(d)
     ok = j2 > 0
     n = d / np.sqrt(np.where(ok, j2, 1.0))[:, None]
-    q = np.empty_like(n)
-    q[:, 0] = n[:, 0] ** 2 + n[:, 3] ** 2 + n[:, 4] ** 2
-    q[:, 1] = n[:, 3] ** 2 + n[:, 1] ** 2 + n[:, 5] ** 2
-    q[:, 2] = n[:, 4] ** 2 + n[:, 5] ** 2 + n[:, 2] ** 2
-    q[:, 3] = n[:, 0] * n[:, 3] + n[:, 3] * n[:, 1] + n[:, 4] * n[:, 5]
-    q[:, 4] = n[:, 0] * n[:, 4] + n[:, 3] * n[:, 5] + n[:, 4] * n[:, 2]
-    q[:, 5] = n[:, 3] * n[:, 4] + n[:, 1] * n[:, 5] + n[:, 5] * n[:, 2]
-    q = _dev(q)
+    N = _mat(n)
+    NN = N @ N
+    q = _dev(np.stack([NN[:, 0, 0], NN[:, 1, 1], NN[:, 2, 2], NN[:, 0, 1], NN[:, 0, 2], NN[:, 1, 2]], 1))
+    lam = np.zeros((len(trial), 3))
+    lam[ok] = np.linalg.eigvalsh(N[ok])
+    return n, q, lam, ok
+
+
+def pole(lam):
+    """(3 l_min^2 - 1)(3 l_max^2 - 1): zero where the least or the most
+    compressive principal direction of the trial is not unique."""
+    return (3 * lam[:, 0] ** 2 - 1) * (3 * lam[:, 2] ** 2 - 1)
+
+
+def features(trial, T, pls, pls_sat):
+    """The raw network inputs (padded to 16): the principal values of the
+    unit trial deviator, T and the plastic strain capped at pls_sat."""
+    n, q, lam, ok = basis(trial)
     raw = np.zeros((len(trial), abi.MLP_IN))
-    raw[:, 0:6] = n
-    raw[:, 6:12] = q
-    raw[:, 12] = T
-    raw[:, 13] = np.minimum(pls, pls_sat)
+    raw[:, 0:3] = lam
+    raw[:, 3] = T
+    raw[:, 4] = np.minimum(pls, pls_sat)
     return raw, ok
 
 
 def targets(rec, trial, shearm):
-    """Network targets: the return per unit multiplier and depls/|alam|."""
+    """Network targets from the logged returns.  The return per unit plastic
+    multiplier R = (trial - new stress) / (2 G alam) is an isotropic function
+    of the trial, so R = a I + b n + c dev(n n) (Cayley-Hamilton); b and c
+    have poles where two principal values meet, so the targets are a,
+    b D, c D with D = pole(eigenvalues of n), and depls / |alam|."""
     depls = rec[:, 20].astype(np.float64)
     anpsi = rec[:, 23].astype(np.float64)
-    c = np.sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18)
-    alam = -depls / c            # a shear return has fs < 0, so alam < 0
+    cdep = np.sqrt((7 + 4 * anpsi + 7 * anpsi * anpsi) / 18)
+    alam = -depls / cdep            # a shear return has fs < 0, so alam < 0
+    R = (trial - rec[:, 14:20]) / (2.0 * shearm * np.where(alam != 0, alam, 1.0))[:, None]
+    n, q, lam, ok = basis(trial)
+    a = R[:, :3].mean(1)
+    Rd = _dev(R)
+    g11, g12, g22 = _inner(n, n), _inner(n, q), _inner(q, q)
+    r1, r2 = _inner(Rd, n), _inner(Rd, q)
+    det = g11 * g22 - g12 * g12
+    good = ok & (depls > 0) & (det > 1e-12)
+    det = np.where(good, det, 1.0)
+    b = (r1 * g22 - r2 * g12) / det
+    c = (r2 * g11 - r1 * g12) / det
+    rebuilt = a[:, None] * np.array([1, 1, 1, 0, 0, 0]) + b[:, None] * n + c[:, None] * q
+    good &= np.linalg.norm(rebuilt - R, axis=1) <= 1e-4 * np.linalg.norm(R, axis=1)
+    D = pole(lam)
     y = np.zeros((len(rec), abi.MLP_OUT))
-    y[:, 0:6] = (trial - rec[:, 14:20]) / (2.0 * shearm * alam)[:, None]
-    y[:, 6] = c
-    return y, depls > 0
+    y[:, 0] = a
+    y[:, 1] = b * D
+    y[:, 2] = c * D
+    y[:, 3] = cdep
+    return y, good
+
+
+def rebuild(y, trial):
+    """The return per unit multiplier from (unscaled) network outputs."""
+    n, q, lam, ok = basis(trial)
+    D = pole(lam)
+    return y[:, 0:1] * np.array([1, 1, 1, 0, 0, 0]) + (y[:, 1] / D)[:, None] * n + (y[:, 2] / D)[:, None] * q
 
 
 def dataset(rec, params):
@@ -117,12 +167,11 @@ def new_net(seed, tol=1e-3):
 
 
 def fit_normalisation(net, raw, y, margin=0.02):
-    """Input mean/scale (directions stay as they are), output scales and the
-    training envelope of the normalised inputs, widened by `margin` of its
-    range."""
+    """Input mean/scale, output scales and the training envelope of the
+    normalised inputs, widened by `margin` of its range."""
     mean = np.zeros(abi.MLP_IN)
     scale = np.ones(abi.MLP_IN)
-    for i in (12, 13):
+    for i in range(USED_IN):
         mean[i] = raw[:, i].mean()
         sd = raw[:, i].std()
         scale[i] = 1.0 / sd if sd > 0 else 1.0
@@ -130,7 +179,9 @@ def fit_normalisation(net, raw, y, margin=0.02):
     lo, hi = x.min(0), x.max(0)
     pad = margin * np.maximum(hi - lo, 1e-3)
     osc = np.ones(abi.MLP_OUT)
-    osc[:NOUT] = np.maximum(np.abs(y[:, :NOUT]).std(0), 1e-6)
+    # outputs that hardly vary (the isotropic part, depls/|alam| once the
+    # dilation has weakened) are scaled by their size instead of their spread
+    osc[:NOUT] = np.maximum(np.maximum(y[:, :NOUT].std(0), 0.1 * np.abs(y[:, :NOUT].mean(0))), 1e-6)
     net.arr("in_mean")[:] = mean
     net.arr("in_scale")[:] = scale
     net.arr("env_lo")[:] = lo - pad

@@ -269,16 +269,17 @@ int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; 
 /* ---- learned return-map closure (no reference counterpart) -------------- */
 /* A 14 -> 64 -> 64 -> 7 MLP with ReLU (inputs padded to 16, outputs to 8),
  * BF16 weights and activations with FP32 accumulation on the tensor cores.
- * It stands in for the Mohr-Coulomb return (rheology.cxx:180-240) of the
- * FP32 form.  Inputs, functions of the element's old stress, strain
- * increment, mean temperature and plastic strain: the direction n of the
- * elastic trial's deviator (6), dev(n n) (6), T and the plastic strain
- * (capped at the largest pls1), normalised as x = (raw - in_mean) *
- * in_scale.  Outputs: (trial - new stress) / (2 G alam) (6) and the
- * plastic-strain increment / |alam| (1), raw = y * out_scale, where alam is
- * the plastic multiplier of the trial's FP32 principal stresses.  Weights
- * are [out][in].  The des_mlp_* calls below take x and y already
- * normalised. */
+ * It stands in for the Mohr-Coulomb shear return (rheology.cxx:180-240) of
+ * the FP32 form.  Inputs (5 used), functions of the element's old stress,
+ * strain increment, temperature and plastic strain: the principal values of
+ * the unit deviator n of the elastic trial, T, and the plastic strain capped
+ * at the largest pls1; x = (raw - in_mean) * in_scale.  Outputs (4 used):
+ * a, b D, c D and depls / |alam| with raw = y * out_scale, where the return
+ * per unit plastic multiplier is (trial - new stress) / (2 G alam) =
+ * a I + b n + c dev(n n) and D = (3 l_min^2 - 1)(3 l_max^2 - 1) clears the
+ * poles of b and c; alam comes from the FP32 principal values of the
+ * trial.  Weights are [out][in].  The des_mlp_* calls below take x and y
+ * already normalised. */
 #define DES_MLP_IN  16
 #define DES_MLP_HID 64
 #define DES_MLP_OUT 8

@@ -103,30 +103,34 @@ def _records(n, seed):
 
 
 def test_targets_reproduce_the_return():
-    """Rebuilding the new stress from the targets returns the oracle's own
-    output, and the return per multiplier is a function of the trial's
-    principal directions alone: with anpsi = 1 it is E_min - E_max, the
-    difference of the projectors on the least and most compressive axes."""
+    """The targets rebuild the oracle's own return: R = a I + (b n + c dev(n n)) / D
+    with the pole factor D, and the return per multiplier is a function of the
+    trial's principal directions alone (with anpsi = 1 it is E_min - E_max, the
+    difference of the projectors on the least and most compressive axes)."""
     rec = _records(200, 11)
     K, G = 128e9, 30e9
     trial = closure.trial_stress(rec, K, G)
     y, ok = closure.targets(rec, trial, G)
     assert ok.all()
-    c = y[:, 6]
-    alam = -rec[:, 20].astype(np.float64) / c
-    rebuilt = trial - 2 * G * alam[:, None] * y[:, :6]
+    R = closure.rebuild(y, trial)
+    alam = -rec[:, 20].astype(np.float64) / y[:, 3]
+    rebuilt = trial - 2 * G * alam[:, None] * R
     scale = np.abs(rec[:, 14:20]).max(1)
     assert (np.abs(rebuilt - rec[:, 14:20]).max(1) / scale).max() < 1e-5
-    # the isotropic part of the return per multiplier is K (1 - anpsi) / G / 2 = 0 here
-    assert np.abs(y[:, :3].mean(1)).max() < 1e-4
+    # the isotropic part of the return per multiplier is K (1 - anpsi) / (2 G) = 0 here
+    assert np.abs(y[:, 0]).max() < 1e-4
     M = np.zeros((len(trial), 3, 3))
     for k, (i, j) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
         M[:, i, j] = M[:, j, i] = trial[:, k]
     _, V = np.linalg.eigh(M)
     P = np.einsum("ni,nj->nij", V[:, :, 0], V[:, :, 0]) - np.einsum("ni,nj->nij", V[:, :, 2], V[:, :, 2])
     Pv = np.stack([P[:, 0, 0], P[:, 1, 1], P[:, 2, 2], P[:, 0, 1], P[:, 0, 2], P[:, 1, 2]], 1)
-    assert np.abs(Pv - y[:, :6]).max() < 1e-4
+    assert np.abs(Pv - R).max() < 1e-4
+    # the pole-cleared coefficients stay bounded
+    assert np.abs(y[:, 1:3]).max() < 10
     raw, ok = closure.features(trial, rec[:, 12], rec[:, 13], 0.1)
     assert ok.all()
-    assert np.allclose((raw[:, :6] ** 2)[:, :3].sum(1) * 0.5 + (raw[:, 3:6] ** 2).sum(1), 1.0)
-    assert raw[:, 13].max() == pytest.approx(0.1)
+    lam = raw[:, 0:3]
+    assert np.allclose(lam.sum(1), 0, atol=1e-12) and np.allclose((lam ** 2).sum(1), 2.0)
+    assert np.all(np.diff(lam, axis=1) >= 0)
+    assert raw[:, 4].max() == pytest.approx(0.1) and np.all(raw[:, 5:] == 0)
