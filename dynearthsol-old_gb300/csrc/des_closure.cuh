@@ -22,10 +22,12 @@
 // compacted onto the first threads of the CTA, which run the FP64 return
 // map, so that the FP64 work is not spread over every warp.
 //
-// Network input (14, normalised as x = (raw - in_mean) * in_scale; 5 used),
-// functions of the old stress, the strain increment, T and plastic strain:
+// Network input (14; 10 used): five quantities, functions of the old stress,
+// the strain increment, T and plastic strain,
 //   the principal values of the unit deviator n of the elastic trial   3
 //   element temperature, plastic strain capped at the largest pls1      2
+// normalised as x = (raw - in_mean) * in_scale, each entering as a pair of
+// BF16 values (x = hi + lo / 256).
 // Network output (7, raw = y * out_scale; 4 used): a, b D, c D and
 // depls / |alam|, where the return per unit plastic multiplier is
 //   R = (trial - new stress) / (2 G alam) = a I + b n + c dev(n n)
@@ -232,7 +234,17 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                     raw[i] = (raw[i] - net->in_mean[i]) * net->in_scale[i];
                     inside = inside && raw[i] >= net->env_lo[i] && raw[i] <= net->env_hi[i];
                 }
-                if (inside) kind = 1;
+                if (inside) {
+                    kind = 1;
+                    // each input enters as a BF16 pair, x = hi + lo / 256, so that
+                    // the network sees it to about 16 significant bits
+                    for (int i = 4; i >= 0; --i) {
+                        const float x = raw[i];
+                        const float hi = __bfloat162float(__float2bfloat16(x));
+                        raw[2 * i] = hi;
+                        raw[2 * i + 1] = (x - hi) * 256.f;
+                    }
+                }
             }
             for (int i = 0; i < 6; ++i) {
                 S.so[i][tid] = so[i];

@@ -153,11 +153,13 @@ def dataset(rec, params):
 
 
 def new_net(seed, tol=1e-3):
-    """He-initialised network (zero padding rows and columns)."""
+    """He-initialised network (zero padding rows and columns, unused inputs)."""
     rng = np.random.default_rng(seed)
     net = abi.Mlp()
     w1 = net.arr("w1")
-    w1[:, :NIN] = rng.normal(0, np.sqrt(2.0 / NIN), (abi.MLP_HID, NIN))
+    w1[:, :2 * USED_IN:2] = rng.normal(0, np.sqrt(2.0 / USED_IN), (abi.MLP_HID, USED_IN))
+    # the low half of each input pair starts with the weight that reassembles x
+    w1[:, 1:2 * USED_IN:2] = w1[:, :2 * USED_IN:2] / 256.0
     net.arr("w2")[:] = rng.normal(0, np.sqrt(2.0 / abi.MLP_HID), (abi.MLP_HID, abi.MLP_HID))
     net.arr("w3")[:NOUT] = rng.normal(0, np.sqrt(1.0 / abi.MLP_HID), (NOUT, abi.MLP_HID))
     net.arr("in_scale")[:] = 1.0
@@ -190,9 +192,22 @@ def fit_normalisation(net, raw, y, margin=0.02):
     return net
 
 
+def _bf16(a):
+    """float32 values rounded to the nearest bfloat16 (ties to even)."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32)
+
+
 def normalise(net, raw, y=None):
-    x = ((raw - net.arr("in_mean")) * net.arr("in_scale")).astype(np.float32)
-    x[:, NIN:] = 0
+    """Network inputs: the normalised quantities, each as a BF16 pair
+    (x = hi + lo / 256, as the stress pass forms them), and scaled targets."""
+    z = ((raw - net.arr("in_mean")) * net.arr("in_scale")).astype(np.float32)
+    x = np.zeros_like(z)
+    for i in range(USED_IN):
+        hi = _bf16(z[:, i])
+        x[:, 2 * i] = hi
+        x[:, 2 * i + 1] = (z[:, i] - hi) * np.float32(256)
     if y is None:
         return np.ascontiguousarray(x)
     t = (y / net.arr("out_scale")).astype(np.float32)
