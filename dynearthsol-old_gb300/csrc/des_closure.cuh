@@ -22,12 +22,13 @@
 // compacted onto the first threads of the CTA, which run the FP64 return
 // map, so that the FP64 work is not spread over every warp.
 //
-// Network input (14; 10 used): five quantities, functions of the old stress,
-// the strain increment, T and plastic strain,
+// Network input (14; 8 used): four quantities, functions of the old stress,
+// the strain increment and the plastic strain,
 //   the principal values of the unit deviator n of the elastic trial   3
-//   element temperature, plastic strain capped at the largest pls1      2
+//   plastic strain capped at the largest pls1                           1
 // normalised as x = (raw - in_mean) * in_scale, each entering as a pair of
-// BF16 values (x = hi + lo / 256).
+// BF16 values (x = hi + lo / 256).  The temperature does not enter the
+// shear return (it acts through the viscosity, outside the network).
 // Network output (7, raw = y * out_scale; 4 used): a, b D, c D and
 // depls / |alam|, where the return per unit plastic multiplier is
 //   R = (trial - new stress) / (2 G alam) = a I + b n + c dev(n n)
@@ -226,9 +227,8 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                 raw[0] = lam[0];
                 raw[1] = lam[1];
                 raw[2] = lam[2];
-                raw[3] = Te;
-                raw[4] = fminf(plsf, pls_sat);
-                for (int i = 5; i < kMlpIn; ++i) raw[i] = 0.f;
+                raw[3] = fminf(plsf, pls_sat);
+                for (int i = 4; i < kMlpIn; ++i) raw[i] = 0.f;
                 bool inside = true;
                 for (int i = 0; i < kMlpInUsed; ++i) {
                     raw[i] = (raw[i] - net->in_mean[i]) * net->in_scale[i];
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                     kind = 1;
                     // each input enters as a BF16 pair, x = hi + lo / 256, so that
                     // the network sees it to about 16 significant bits
-                    for (int i = 4; i >= 0; --i) {
+                    for (int i = 3; i >= 0; --i) {
                         const float x = raw[i];
                         const float hi = __bfloat162float(__float2bfloat16(x));
                         raw[2 * i] = hi;

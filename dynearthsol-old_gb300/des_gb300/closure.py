@@ -13,7 +13,7 @@ import numpy as np
 from . import abi
 
 NIN, NOUT = 14, 7
-USED_IN, USED_OUT = 5, 4     # inputs and outputs the closure uses (the rest are zero)
+USED_IN, USED_OUT = 4, 4     # quantities in and out that the closure uses (the rest are zero)
 _FP = C.POINTER(C.c_float)
 
 
@@ -94,12 +94,15 @@ def pole(lam):
 
 def features(trial, T, pls, pls_sat):
     """The raw network inputs (padded to 16): the principal values of the
-    unit trial deviator, T and the plastic strain capped at pls_sat."""
+    unit trial deviator and the plastic strain capped at pls_sat.  The
+    temperature T is part of the record but does not enter the shear return
+    (it acts through the viscosity, outside the network), so it is not an
+    input: a network that saw it would pick up the geotherm of its training
+    box."""
     n, q, lam, ok = basis(trial)
     raw = np.zeros((len(trial), abi.MLP_IN))
     raw[:, 0:3] = lam
-    raw[:, 3] = T
-    raw[:, 4] = np.minimum(pls, pls_sat)
+    raw[:, 3] = np.minimum(pls, pls_sat)
     return raw, ok
 
 

@@ -270,10 +270,11 @@ int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; 
 /* A 14 -> 64 -> 64 -> 7 MLP with ReLU (inputs padded to 16, outputs to 8),
  * BF16 weights and activations with FP32 accumulation on the tensor cores.
  * It stands in for the Mohr-Coulomb shear return (rheology.cxx:180-240) of
- * the FP32 form.  Inputs (5 used), functions of the element's old stress,
- * strain increment, temperature and plastic strain: the principal values of
- * the unit deviator n of the elastic trial, T, and the plastic strain capped
- * at the largest pls1; x = (raw - in_mean) * in_scale.  Outputs (4 used):
+ * the FP32 form.  Inputs (8 used), functions of the element's old stress,
+ * strain increment and plastic strain: the principal values of the unit
+ * deviator n of the elastic trial and the plastic strain capped at the
+ * largest pls1, x = (raw - in_mean) * in_scale, each as a BF16 pair
+ * (hi, 256 lo) (the temperature does not enter the shear return).  Outputs (4 used):
  * a, b D, c D and depls / |alam| with raw = y * out_scale, where the return
  * per unit plastic multiplier is (trial - new stress) / (2 G alam) =
  * a I + b n + c dev(n n) and D = (3 l_min^2 - 1)(3 l_max^2 - 1) clears the

@@ -133,4 +133,4 @@ def test_targets_reproduce_the_return():
     lam = raw[:, 0:3]
     assert np.allclose(lam.sum(1), 0, atol=1e-12) and np.allclose((lam ** 2).sum(1), 2.0)
     assert np.all(np.diff(lam, axis=1) >= 0)
-    assert raw[:, 4].max() == pytest.approx(0.1) and np.all(raw[:, 5:] == 0)
+    assert raw[:, 3].max() == pytest.approx(0.1) and np.all(raw[:, 4:] == 0)
