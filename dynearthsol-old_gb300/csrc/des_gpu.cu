@@ -50,6 +50,9 @@ struct des_gpu {
     MlpDev *dnet = nullptr;      // the learned closure (FP32 form), when set
     bool closure = false;
     unsigned long long *qout = nullptr;   // mesh-quality reductions
+    int avg_interval = 0;                 // Output::average_fields every step when > 0
+    double *avg_c0 = nullptr, *avg_strain0 = nullptr, *avg_stress = nullptr, *avg_dpls = nullptr,
+           *avg_time0 = nullptr;
 };
 
 namespace {
@@ -475,6 +478,29 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
         k_fe_a<<<eb, kElemBlock, 0, st>>>(d);
     }
     if (ev) cudaEventRecord(ev[6], st);
+    if (g->avg_interval > 0) {
+        AvgArgs a;
+        a.nnode = g->nnode;
+        a.nelem = g->nelem;
+        a.interval = g->avg_interval;
+        a.clk = g->dclk;
+        a.coord = g->d.x;
+        const bool f32 = g->prec == DES_PREC_FP32;
+        a.stress = f32 ? nullptr : g->d.stress;
+        a.strain = f32 ? nullptr : g->d.strain;
+        a.dpls = f32 ? nullptr : g->d.dpls;
+        a.stress_f = f32 ? g->f.stress : nullptr;
+        a.strain_f = f32 ? g->f.strain : nullptr;
+        a.dpls_f = f32 ? g->f.dpls : nullptr;
+        a.s0 = f32 ? g->f.s0 : nullptr;
+        a.c0 = g->avg_c0;
+        a.strain0 = g->avg_strain0;
+        a.stress_sum = g->avg_stress;
+        a.dpls_sum = g->avg_dpls;
+        a.time0 = g->avg_time0;
+        const long long n = std::max(3LL * g->nnode, (long long)g->nelem);
+        k_average_fields<<<blocks(n, 256), 256, 0, st>>>(a);
+    }
 }
 
 int finish(des_gpu *g)
@@ -989,6 +1015,37 @@ int des_gpu_elem_quality(des_gpu *g, double *quality)
     DES_CUDA(cudaMemcpyAsync(quality, q, sizeof(double) * g->nelem, cudaMemcpyDeviceToHost, g->stream));
     DES_CUDA(cudaStreamSynchronize(g->stream));
     return DES_OK;
+}
+
+int des_gpu_set_averaging(des_gpu *g, int interval)
+{
+    if (!g || interval < 0) return DES_ERR_ARG;
+    if (interval > 0 && !g->avg_c0) {
+        const size_t N = g->nnode, E = g->nelem;
+        int rc;
+        if ((rc = dev_alloc(g, &g->avg_c0, 3 * N)) || (rc = dev_alloc(g, &g->avg_strain0, 6 * E)) ||
+            (rc = dev_alloc(g, &g->avg_stress, 6 * E)) || (rc = dev_alloc(g, &g->avg_dpls, E)) ||
+            (rc = dev_alloc(g, &g->avg_time0, 1)))
+            return rc;
+    }
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+    g->avg_interval = interval;
+    return DES_OK;
+}
+
+int des_gpu_download_averages(des_gpu *g, double *coord0, double *strain0, double *stress_sum,
+                              double *dpls_sum, double *time0)
+{
+    if (!g) return DES_ERR_ARG;
+    if (!g->avg_c0) return DES_ERR_UNSUPPORTED;
+    int rc;
+    if (coord0 && (rc = download_field(g, coord0, g->avg_c0, 3, g->nnode))) return rc;
+    if (strain0 && (rc = download_field(g, strain0, g->avg_strain0, 6, g->nelem))) return rc;
+    if (stress_sum && (rc = download_field(g, stress_sum, g->avg_stress, 6, g->nelem))) return rc;
+    if (dpls_sum && (rc = download_field(g, dpls_sum, g->avg_dpls, 1, g->nelem))) return rc;
+    if (time0) DES_CUDA(cudaMemcpyAsync(time0, g->avg_time0, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
+    return finish(g);
 }
 
 int des_gpu_set_closure(des_gpu *g, const des_mlp *net)

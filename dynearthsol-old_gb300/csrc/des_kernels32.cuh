@@ -824,6 +824,49 @@ __global__ void k_stress_split_tiled(const double *src, double *s0, float *dst, 
     for (int c = 0; c < 6; ++c) dst[c * rows + r0 + r] = (float)(a[c] - (c < 3 ? m : 0.0));
 }
 
+// ---- Output::average_fields (output.cxx:227-267) after a step ---------------
+// Both forms: the element sources are FP64 arrays or FP32 arrays (the FP32
+// stress adding the reference stress s0 back).
+struct AvgArgs {
+    int nnode, nelem, interval;
+    const Clock *clk;
+    const double *coord;                        // SoA x | y | z
+    const double *stress, *strain, *dpls;       // FP64 form
+    const float *stress_f, *strain_f, *dpls_f;  // FP32 form
+    const double *s0;
+    double *c0, *strain0, *stress_sum, *dpls_sum, *time0;
+};
+__global__ void k_average_fields(AvgArgs a)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool first = (a.clk->steps % a.interval) == 1;
+    if (i == 0 && first) *a.time0 = a.clk->time;
+    if (first && i < 3LL * a.nnode) a.c0[i] = a.coord[i];
+    if (i >= a.nelem) return;
+    const size_t E = a.nelem;
+    for (int c = 0; c < 6; ++c) {
+        double sv, ev;
+        if (a.stress) {
+            sv = a.stress[c * E + i];
+            ev = a.strain[c * E + i];
+        } else {
+            sv = (double)a.stress_f[c * E + i] + (c < 3 ? a.s0[i] : 0.0);
+            ev = (double)a.strain_f[c * E + i];
+        }
+        if (first) {
+            a.strain0[c * E + i] = ev;
+            a.stress_sum[c * E + i] = sv;
+        } else {
+            a.stress_sum[c * E + i] += sv;
+        }
+    }
+    const double dp = a.dpls ? a.dpls[i] : (double)a.dpls_f[i];
+    if (first)
+        a.dpls_sum[i] = dp;
+    else
+        a.dpls_sum[i] += dp;
+}
+
 __global__ void k_vol_to_f(const double *vol, float *volf, long long n)
 {
     long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;

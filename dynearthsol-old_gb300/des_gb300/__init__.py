@@ -80,6 +80,10 @@ def lib():
     L.des_gpu_bad_mesh_quality.argtypes = [C.c_void_p, P(abi.RemeshCheck), P(C.c_int), P(C.c_int),
                                            P(C.c_double)]
     L.des_gpu_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
+    L.des_write_save.argtypes = [C.c_char_p, P(abi.MeshView), P(abi.Params), P(C.c_uint),
+                                 P(abi.StateView), P(abi.SaveAverages)]
+    L.des_gpu_set_averaging.argtypes = [C.c_void_p, C.c_int]
+    L.des_gpu_download_averages.argtypes = [C.c_void_p] + [P(C.c_double)] * 5
     _lib = L
     return L
 
@@ -218,6 +222,23 @@ class Device:
         _ck(self.L.des_gpu_elem_quality(self.h, abi.dptr(q)), "des_gpu_elem_quality")
         return q
 
+    def set_averaging(self, interval):
+        """Output::average_fields after every step (0 stops it)."""
+        _ck(self.L.des_gpu_set_averaging(self.h, interval), "des_gpu_set_averaging")
+
+    def download_averages(self, interval):
+        """The device's averaging state as an abi.SaveAverages (with the
+        numpy arrays it points into kept alive on the object)."""
+        N, E = self.mesh.nnode, self.mesh.nelem
+        arr = dict(coord0=np.zeros((N, 3)), strain0=np.zeros((E, 6)), stress_sum=np.zeros((E, 6)),
+                   dpls_sum=np.zeros(E))
+        t0 = C.c_double()
+        _ck(self.L.des_gpu_download_averages(self.h, *(abi.dptr(arr[k]) for k in
+                                                      ("coord0", "strain0", "stress_sum", "dpls_sum")),
+                                             C.byref(t0)), "des_gpu_download_averages")
+        return save_averages(arr["coord0"], arr["strain0"], arr["stress_sum"], arr["dpls_sum"],
+                             t0.value, interval)
+
     def set_closure(self, net):
         """Installs an abi.Mlp as the learned closure (None removes it)."""
         _ck(lib().des_gpu_set_closure(self.h, C.byref(net) if net is not None else None),
@@ -230,6 +251,25 @@ class Device:
     @property
     def device_bytes(self):
         return self.L.des_gpu_device_bytes(self.h)
+
+
+def save_averages(coord0, strain0, stress_sum, dpls_sum, time0, interval):
+    """An abi.SaveAverages over numpy arrays (kept alive on it)."""
+    a = abi.SaveAverages()
+    a._keep = [np.ascontiguousarray(x, dtype=np.float64) for x in (coord0, strain0, stress_sum, dpls_sum)]
+    a.coord0, a.strain0, a.stress_sum, a.dpls_sum = (abi.dptr(x) for x in a._keep)
+    a.time0 = time0
+    a.interval = interval
+    return a
+
+
+def write_save(path, mesh, params, bcflag, state, averages=None):
+    """The .save file of one output frame (des_write_save)."""
+    v = state.view()
+    mv = mesh.view()
+    b = np.ascontiguousarray(bcflag, dtype=np.uint32)
+    _ck(lib().des_write_save(str(path).encode(), C.byref(mv), C.byref(params), abi.uptr(b), C.byref(v),
+                             C.byref(averages) if averages is not None else None), "des_write_save")
 
 
 def pin(state):

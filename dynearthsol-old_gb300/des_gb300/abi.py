@@ -129,6 +129,12 @@ class StepReport(C.Structure):
                 ("closure_accepted", C.c_longlong), ("exact_returns", C.c_longlong)]
 
 
+class SaveAverages(C.Structure):
+    """des_save_averages: the averaging state of Output::average_fields."""
+    _fields_ = [("coord0", _dp), ("strain0", _dp), ("stress_sum", _dp), ("dpls_sum", _dp),
+                ("time0", C.c_double), ("interval", C.c_int)]
+
+
 class RemeshCheck(C.Structure):
     """des_remesh_check: the mesh.* parameters of bad_mesh_quality."""
     _fields_ = [("smallest_size", C.c_double), ("resolution", C.c_double), ("zlength", C.c_double),

@@ -23,7 +23,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", ARCH, "-lineinfo", "-fmad=false", "--extended
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", f"-I{INCLUDE}"]
 
 CU_SOURCES = ["des_gpu.cu", "des_noalloc.cu", "des_mlp.cu"]
-CXX_SOURCES = ["topology.cpp", "workload.cpp"]
+CXX_SOURCES = ["topology.cpp", "workload.cpp", "save.cpp"]
 
 
 def _nvcc():

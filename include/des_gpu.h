@@ -307,6 +307,33 @@ int  des_mlp_loss_grad(const des_mlp *net, const float *x, const float *y, long 
 int  des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int steps,
                    int batch, float lr, unsigned long long seed, float *loss_trace);
 
+/* ---- output frames ------------------------------------------------------ */
+/* The state of Output::average_fields (output.cxx:227-267) over the current
+ * averaging interval, AoS host arrays. */
+typedef struct des_save_averages {
+    const double *coord0;       /* [nnode][3] coordinates at the interval's first step */
+    const double *strain0;      /* [nelem][6] strain at the interval's first step */
+    const double *stress_sum;   /* [nelem][6] stress summed over the interval */
+    const double *dpls_sum;     /* [nelem]    plastic-strain increments summed */
+    double time0;               /* time at the interval's first step */
+    int    interval;            /* mesh.quality_check_step_interval */
+} des_save_averages;
+
+/* Writes the .save file of one output frame to `path` as Output::_write
+ * (output.cxx:73-198, BinaryOutput binaryio.cxx:44-131) does, byte for byte,
+ * without marker sets: avg NULL for Output::write_exact or when averaging is
+ * off.  Density, mesh quality, viscosity and material are computed on the
+ * host with the reference's arithmetic.  Host-only; needs no GPU. */
+int  des_write_save(const char *path, const des_mesh_view *mesh, const des_params *p,
+                    const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg);
+
+/* Output::average_fields on the device after every step from the next
+ * des_gpu_step on (interval = mesh.quality_check_step_interval; 0 stops it). */
+int  des_gpu_set_averaging(des_gpu *g, int interval);
+/* The averaging state into host AoS arrays (any may be NULL) and *time0. */
+int  des_gpu_download_averages(des_gpu *g, double *coord0, double *strain0, double *stress_sum,
+                               double *dpls_sum, double *time0);
+
 /* ---- remesh trigger: bad_mesh_quality on the device ------------------- */
 typedef struct des_remesh_check {
     double smallest_size;            /* mesh.smallest_size */

@@ -223,6 +223,8 @@ class RefOracle(_Base):
             L.dsr_bfacets.argtypes = [C.c_void_p, C.c_int, P(C.c_int), P(C.c_int)]
             L.dsr_normals.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
             L.dsr_dsyevh3.argtypes = [P(C.c_double)] * 3
+            L.dsr_output_begin.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]
+            L.dsr_output_write.argtypes = [C.c_void_p, C.c_int]
             L.dsr_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
             L.dsr_worst_elem_quality.argtypes = [C.c_void_p, P(C.c_int)]
             L.dsr_worst_elem_quality.restype = C.c_double
@@ -289,6 +291,18 @@ class RefOracle(_Base):
         self.L.dsr_bfacets(self.h, b, C.byref(n), abi.iptr(a))
         return a
 
+    def output_begin(self, modelname, frame=0, averaged=False, interval=1):
+        """The reference's Output for `modelname` (averaging in every later
+        step when averaged)."""
+        self.L.dsr_output_begin(self.h, str(modelname).encode(), frame, int(averaged), interval)
+
+    def output_write(self, state, exact=False):
+        """Output::write (write_exact) of `state`: <modelname>.save.<frame>."""
+        self._in(state)
+        rc = self.L.dsr_output_write(self.h, int(exact))
+        if rc:
+            raise RuntimeError("output not set up")
+
     def elem_quality(self, state):
         """The reference's elem_quality of every element, and its
         worst_elem_quality (value, index)."""
@@ -315,3 +329,24 @@ def dsyevh3(a, which="port"):
     fn = L.dso_dsyevh3 if which == "port" else L.dsr_dsyevh3
     rc = fn(abi.dptr(a), abi.dptr(q), abi.dptr(w))
     return rc, q.reshape(3, 3), w
+
+
+class Averages:
+    """Output::average_fields (output.cxx:227-267) restated over AoS states:
+    call update(state) after every step."""
+
+    def __init__(self, interval):
+        self.interval = interval
+        self.coord0 = self.strain0 = self.stress_sum = self.dpls_sum = None
+        self.time0 = 0.0
+
+    def update(self, s):
+        if s.steps % self.interval == 1:
+            self.time0 = s.time
+            self.coord0 = s.coord.copy()
+            self.strain0 = s.strain.copy()
+            self.stress_sum = s.stress.copy()
+            self.dpls_sum = s.delta_plstrain.copy()
+        else:
+            self.stress_sum += s.stress
+            self.dpls_sum += s.delta_plstrain

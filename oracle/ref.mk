@@ -13,7 +13,7 @@ CXX    ?= g++
 BASE   := -std=c++0x -fPIC -fopenmp -DTHREED -I$(REF) -I$(REF)/ann/include -w
 CXXFLAGS := $(BASE) -O2
 
-DES_SRCS := fields geometry rheology matprops bc mesh markerset barycentric-fn binaryio \
+DES_SRCS := fields geometry rheology matprops bc mesh markerset barycentric-fn binaryio output \
             ic ic-read-temp brc-interpolation phasechanges
 C3X3     := dsytrd3 dsyevc3 dsyevq3 dsyevh3
 ANN_SRCS := ANN brute kd_tree kd_util kd_split kd_dump kd_search kd_pr_search \

@@ -19,6 +19,7 @@
 #include "ic.hpp"
 #include "matprops.hpp"
 #include "mesh.hpp"
+#include "output.hpp"
 #include "rheology.hpp"
 #include "3x3-C/dsyevh3.h"
 
@@ -27,6 +28,7 @@
 struct dsr {
     Param param;
     Variables var;
+    Output *out = nullptr;       // the reference's own output writer, when set up
 };
 
 namespace {
@@ -385,6 +387,7 @@ int dsr_step(dsr *h, int nsteps)
         dsr_update_mesh(h);
         if (var.mat->rheol_type & MatProps::rh_elastic) rotate_stress(var, *var.stress, *var.strain);
         if (var.steps % 10 == 0) var.dt = compute_dt(param, var);
+        if (h->out && param.sim.is_outputting_averaged_fields) h->out->average_fields(var);   // dynearthsol.cxx:395-396
     }
     return 0;
 }
@@ -408,6 +411,29 @@ int dsr_elem_quality(const dsr *h, double *quality)
 double dsr_worst_elem_quality(const dsr *h, int *worst)
 {
     return worst_elem_quality(*h->var.coord, *h->var.connectivity, *h->var.volume, *worst);
+}
+
+// Output (output.cxx) for frame `frame` of model `modelname`, averaging over
+// `interval` steps when averaged != 0 (then dsr_step calls average_fields)
+int dsr_output_begin(dsr *h, const char *modelname, int frame, int averaged, int interval)
+{
+    delete h->out;
+    h->param.sim.modelname = modelname;
+    h->param.sim.is_outputting_averaged_fields = averaged != 0;
+    h->param.sim.has_marker_output = false;
+    h->param.mesh.quality_check_step_interval = interval;
+    h->out = new Output(h->param, 0.0, frame);
+    return 0;
+}
+// Output::write (or write_exact) of the current state: <modelname>.save.<frame>
+int dsr_output_write(dsr *h, int exact)
+{
+    if (!h->out) return 1;
+    if (exact)
+        h->out->write_exact(h->var);
+    else
+        h->out->write(h->var);
+    return 0;
 }
 
 void dsr_destroy(dsr *h) { (void)h; /* the reference's arrays are never freed by its own code */ }
