@@ -50,6 +50,14 @@ struct des_gpu {
     MlpDev *dnet = nullptr;      // the learned closure (FP32 form), when set
     bool closure = false;
     unsigned long long *qout = nullptr;   // mesh-quality reductions
+    // output snapshot: the selected fields as FP64 AoS rows in device memory,
+    // copied to the host on their own stream while the steps go on
+    double *snap = nullptr;
+    long long snap_bytes = 0;
+    unsigned snap_mask = 0;
+    Clock *snap_clk = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
     int avg_interval = 0;                 // Output::average_fields every step when > 0
     double *avg_c0 = nullptr, *avg_strain0 = nullptr, *avg_stress = nullptr, *avg_dpls = nullptr,
            *avg_time0 = nullptr;
@@ -721,6 +729,12 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
 int des_gpu_destroy(des_gpu *g)
 {
     if (!g) return DES_OK;
+    if (g->copy_stream) {
+        cudaStreamSynchronize(g->copy_stream);
+        cudaStreamDestroy(g->copy_stream);
+    }
+    if (g->snap_ready) cudaEventDestroy(g->snap_ready);
+    if (g->snap_done) cudaEventDestroy(g->snap_done);
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->graph) cudaGraphExecDestroy(g->graph);
     for (void *p : g->allocs) cudaFree(p);
@@ -1014,6 +1028,129 @@ int des_gpu_elem_quality(des_gpu *g, double *quality)
     if (int rc = run_quality(g, nullptr, &q)) return rc;
     DES_CUDA(cudaMemcpyAsync(quality, q, sizeof(double) * g->nelem, cudaMemcpyDeviceToHost, g->stream));
     DES_CUDA(cudaStreamSynchronize(g->stream));
+    return DES_OK;
+}
+
+// ---- output snapshots ---------------------------------------------------
+// fields a snapshot can hold, in this order, with their AoS row widths
+namespace {
+constexpr unsigned kSnapFields = DES_F_COORD | DES_F_VEL | DES_F_FORCE | DES_F_TEMPERATURE | DES_F_VOLUME |
+                                 DES_F_STRESS | DES_F_STRAIN | DES_F_STRAIN_RATE | DES_F_PLSTRAIN | DES_F_COORD0;
+struct SnapPart {
+    unsigned flag;
+    int ncomp;
+    bool node;
+    double *des_state_view::*host;
+};
+const SnapPart kSnap[] = {
+    {DES_F_COORD, 3, true, &des_state_view::coord},
+    {DES_F_VEL, 3, true, &des_state_view::vel},
+    {DES_F_FORCE, 3, true, &des_state_view::force},
+    {DES_F_TEMPERATURE, 1, true, &des_state_view::temperature},
+    {DES_F_COORD0, 3, true, &des_state_view::coord0},
+    {DES_F_VOLUME, 1, false, &des_state_view::volume},
+    {DES_F_VOLUME, 1, false, &des_state_view::volume_old},
+    {DES_F_STRESS, 6, false, &des_state_view::stress},
+    {DES_F_STRAIN, 6, false, &des_state_view::strain},
+    {DES_F_STRAIN_RATE, 6, false, &des_state_view::strain_rate},
+    {DES_F_PLSTRAIN, 1, false, &des_state_view::plstrain},
+    {DES_F_PLSTRAIN, 1, false, &des_state_view::delta_plstrain},
+};
+}  // namespace
+
+int des_gpu_output_snapshot(des_gpu *g, unsigned mask)
+{
+    if (!g || (mask & ~kSnapFields)) return DES_ERR_ARG;
+    const long long N = g->nnode, E = g->nelem;
+    if (!g->snap) {
+        long long n = 0;
+        for (const SnapPart &s : kSnap) n += (long long)s.ncomp * (s.node ? N : E);
+        int rc;
+        if ((rc = dev_alloc(g, &g->snap, (size_t)n)) || (rc = dev_alloc(g, &g->snap_clk, 1))) return rc;
+        g->snap_bytes = n * (long long)sizeof(double);
+        DES_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+        DES_CUDA(cudaEventCreateWithFlags(&g->snap_ready, cudaEventDisableTiming));
+        DES_CUDA(cudaEventCreateWithFlags(&g->snap_done, cudaEventDisableTiming));
+        DES_CUDA(cudaEventRecord(g->snap_done, g->copy_stream));
+    }
+    // the previous snapshot's copies must have left the buffer
+    DES_CUDA(cudaStreamWaitEvent(g->stream, g->snap_done, 0));
+    const bool f32 = g->prec == DES_PREC_FP32;
+    const Dev &d = g->d;
+    const DevF &f = g->f;
+    double *dst = g->snap;
+    cudaStream_t st = g->stream;
+    for (const SnapPart &s : kSnap) {
+        const long long rows = s.node ? N : E;
+        if (mask & s.flag) {
+            const int nb = blocks(rows * s.ncomp, 256);
+            const bool shared64 = s.host == &des_state_view::coord || s.host == &des_state_view::coord0 ||
+                                  s.host == &des_state_view::temperature || s.host == &des_state_view::volume ||
+                                  s.host == &des_state_view::volume_old || s.host == &des_state_view::plstrain;
+            if (s.host == &des_state_view::stress && f32) {
+                k_stress_join<<<blocks(E, 256), 256, 0, st>>>(f.s0, f.stress, dst, E, 0, E);
+            } else if (shared64 || !f32) {
+                const double *src = s.host == &des_state_view::coord ? d.x
+                                  : s.host == &des_state_view::coord0 ? d.x0
+                                  : s.host == &des_state_view::temperature ? d.T
+                                  : s.host == &des_state_view::volume ? d.vol
+                                  : s.host == &des_state_view::volume_old ? d.vol_old
+                                  : s.host == &des_state_view::plstrain ? d.pls
+                                  : s.host == &des_state_view::vel ? d.vx
+                                  : s.host == &des_state_view::force ? d.fx
+                                  : s.host == &des_state_view::stress ? d.stress
+                                  : s.host == &des_state_view::strain ? d.strain
+                                  : s.host == &des_state_view::strain_rate ? d.srate
+                                  : d.dpls;
+                k_soa_to_aos<<<nb, 256, 0, st>>>(src, dst, s.ncomp, rows, 0, rows);
+            } else {
+                const float *src = s.host == &des_state_view::vel ? f.vx
+                                 : s.host == &des_state_view::force ? f.fx
+                                 : s.host == &des_state_view::strain ? f.strain
+                                 : s.host == &des_state_view::strain_rate ? f.srate
+                                 : f.dpls;
+                k_soa_to_aos_f<<<nb, 256, 0, st>>>(src, dst, s.ncomp, rows, 0, rows);
+            }
+            DES_LAUNCH();
+        }
+        dst += rows * s.ncomp;
+    }
+    DES_CUDA(cudaMemcpyAsync(g->snap_clk, g->dclk, sizeof(Clock), cudaMemcpyDeviceToDevice, st));
+    DES_CUDA(cudaEventRecord(g->snap_ready, st));
+    g->snap_mask = mask;
+    return DES_OK;
+}
+
+int des_gpu_output_fetch(des_gpu *g, des_state_view *h)
+{
+    if (!g || !h || !g->snap || h->nnode != g->nnode || h->nelem != g->nelem) return DES_ERR_ARG;
+    const long long N = g->nnode, E = g->nelem;
+    for (const SnapPart &s : kSnap)
+        if ((g->snap_mask & s.flag) && !(h->*(s.host))) return DES_ERR_ARG;
+    cudaStream_t cs = g->copy_stream;
+    DES_CUDA(cudaStreamWaitEvent(cs, g->snap_ready, 0));
+    const double *src = g->snap;
+    for (const SnapPart &s : kSnap) {
+        const long long n = (s.node ? N : E) * s.ncomp;
+        if (g->snap_mask & s.flag)
+            DES_CUDA(cudaMemcpyAsync(h->*(s.host), src, sizeof(double) * n, cudaMemcpyDeviceToHost, cs));
+        src += n;
+    }
+    DES_CUDA(cudaEventRecord(g->snap_done, cs));
+    return DES_OK;
+}
+
+int des_gpu_output_wait(des_gpu *g, des_state_view *h)
+{
+    if (!g || !g->copy_stream) return DES_ERR_ARG;
+    DES_CUDA(cudaStreamSynchronize(g->copy_stream));
+    if (h) {
+        Clock c;
+        DES_CUDA(cudaMemcpy(&c, g->snap_clk, sizeof(Clock), cudaMemcpyDeviceToHost));
+        h->time = c.time;
+        h->dt = c.dt;
+        h->steps = c.steps;
+    }
     return DES_OK;
 }
 

@@ -83,6 +83,9 @@ def lib():
     L.des_write_save.argtypes = [C.c_char_p, P(abi.MeshView), P(abi.Params), P(C.c_uint),
                                  P(abi.StateView), P(abi.SaveAverages)]
     L.des_gpu_set_averaging.argtypes = [C.c_void_p, C.c_int]
+    L.des_gpu_output_snapshot.argtypes = [C.c_void_p, C.c_uint]
+    L.des_gpu_output_fetch.argtypes = [C.c_void_p, P(abi.StateView)]
+    L.des_gpu_output_wait.argtypes = [C.c_void_p, P(abi.StateView)]
     L.des_gpu_download_averages.argtypes = [C.c_void_p] + [P(C.c_double)] * 5
     _lib = L
     return L
@@ -221,6 +224,26 @@ class Device:
         q = np.zeros(self.mesh.nelem)
         _ck(self.L.des_gpu_elem_quality(self.h, abi.dptr(q)), "des_gpu_elem_quality")
         return q
+
+    OUTPUT_FIELDS = (abi.F_COORD | abi.F_VEL | abi.F_FORCE | abi.F_TEMPERATURE | abi.F_VOLUME |
+                     abi.F_STRESS | abi.F_STRAIN | abi.F_STRAIN_RATE | abi.F_PLSTRAIN | abi.F_COORD0)
+
+    def output_snapshot(self, mask=None):
+        """Copy the output fields on the device (step stream)."""
+        _ck(self.L.des_gpu_output_snapshot(self.h, self.OUTPUT_FIELDS if mask is None else mask),
+            "des_gpu_output_snapshot")
+
+    def output_fetch(self, state):
+        """Start the snapshot's copy into state's arrays (page-locked for
+        overlap); the arrays must stay alive until output_wait."""
+        self._fetch_view = state.view()
+        _ck(self.L.des_gpu_output_fetch(self.h, C.byref(self._fetch_view)), "des_gpu_output_fetch")
+
+    def output_wait(self, state):
+        v = self._fetch_view
+        _ck(self.L.des_gpu_output_wait(self.h, C.byref(v)), "des_gpu_output_wait")
+        state.sync_scalars(v)
+        return state
 
     def set_averaging(self, interval):
         """Output::average_fields after every step (0 stops it)."""

@@ -327,6 +327,19 @@ typedef struct des_save_averages {
 int  des_write_save(const char *path, const des_mesh_view *mesh, const des_params *p,
                     const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg);
 
+/* Asynchronous output (the download of output.cxx's fields overlapped with
+ * the next steps): des_gpu_output_snapshot copies the `mask` fields
+ * (DES_F_COORD, _VEL, _FORCE, _TEMPERATURE, _VOLUME, _STRESS, _STRAIN,
+ * _STRAIN_RATE, _PLSTRAIN, _COORD0) as FP64 rows into device memory on the
+ * step stream; des_gpu_output_fetch starts their copy to the host arrays of
+ * `host` on a second stream and returns; steps may run meanwhile;
+ * des_gpu_output_wait blocks until the copy is done and sets host's time, dt
+ * and steps to the snapshot's.  The copies overlap only into page-locked
+ * host memory (des_host_register). */
+int  des_gpu_output_snapshot(des_gpu *g, unsigned mask);
+int  des_gpu_output_fetch(des_gpu *g, des_state_view *host);
+int  des_gpu_output_wait(des_gpu *g, des_state_view *host);
+
 /* Output::average_fields on the device after every step from the next
  * des_gpu_step on (interval = mesh.quality_check_step_interval; 0 stops it). */
 int  des_gpu_set_averaging(des_gpu *g, int interval);

@@ -60,3 +60,35 @@ def test_fp32_form_averages(gpu):
     ss = np.ctypeslib.as_array(a.stress_sum, shape=avg.stress_sum.shape)
     assert rel_l2(ss, avg.stress_sum) < 1e-5
     assert a.time0 == avg.time0
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_output_snapshot_overlaps_the_steps(gpu, pinned):
+    """A snapshot after 5 steps, fetched while 5 more steps run, holds the
+    state after 5 steps; the stepping is not disturbed."""
+    c = Case(W.CONFIGS["1"])
+    s0 = c.initial_state()
+    dev = c.device()
+    dev.upload(s0, abi.F_ALL)
+    dev.step(5)
+    host = abi.State(c.mesh.nnode, c.mesh.nelem)
+    if pinned:
+        D.pin(host)
+    dev.output_snapshot()
+    dev.output_fetch(host)
+    dev.step(5)
+    dev.output_wait(host)
+    after10 = dev.download(abi.State(c.mesh.nnode, c.mesh.nelem), abi.F_ALL)
+    if pinned:
+        D.unpin(host)
+    dev.close()
+    want5 = s0.copy()
+    c.oracle.step(want5, 5)
+    want10 = want5.copy()
+    c.oracle.step(want10, 5)
+    for f in ("coord", "vel", "force", "temperature", "volume", "volume_old", "stress", "strain",
+              "strain_rate", "plstrain", "delta_plstrain", "coord0"):
+        assert np.array_equal(getattr(host, f), getattr(want5, f)), f
+        if f != "coord0":
+            assert np.array_equal(getattr(after10, f), getattr(want10, f)), f
+    assert (host.steps, host.time, host.dt) == (want5.steps, want5.time, want5.dt)
