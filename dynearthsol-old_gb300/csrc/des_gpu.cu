@@ -800,22 +800,21 @@ int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
             if (const double *m = static_cast<const double *>(mapped(h->stress))) {
                 k_stress_split_tiled<<<blocks(E, 256), 256, 0, g->stream>>>(m, f.s0, f.stress, E);
                 DES_LAUNCH();
-                goto stress_done;
-            }
-            long long chunk = std::max(1LL, g->staging_elems / 6);
-            for (long long r0 = 0; r0 < E; r0 += chunk) {
-                long long nr = std::min(chunk, E - r0);
-                DES_CUDA(cudaMemcpyAsync(g->staging, h->stress + 6 * r0, sizeof(double) * 6 * nr,
-                                         cudaMemcpyHostToDevice, g->stream));
-                k_stress_split<<<blocks(nr, 256), 256, 0, g->stream>>>(g->staging, f.s0, f.stress, nr,
-                                                                        r0, E);
-                DES_LAUNCH();
+            } else {
+                long long chunk = std::max(1LL, g->staging_elems / 6);
+                for (long long r0 = 0; r0 < E; r0 += chunk) {
+                    long long nr = std::min(chunk, E - r0);
+                    DES_CUDA(cudaMemcpyAsync(g->staging, h->stress + 6 * r0, sizeof(double) * 6 * nr,
+                                             cudaMemcpyHostToDevice, g->stream));
+                    k_stress_split<<<blocks(nr, 256), 256, 0, g->stream>>>(g->staging, f.s0, f.stress, nr,
+                                                                            r0, E);
+                    DES_LAUNCH();
+                }
             }
         } else if ((rc = upload_field(g, h->stress, d.stress, 6, E))) {
             return rc;
         }
     }
-stress_done:
     UPX(DES_F_STRAIN, strain, strain, 0, 6, E)
     UPX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
     UP(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
