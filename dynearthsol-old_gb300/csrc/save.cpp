@@ -211,3 +211,20 @@ extern "C" int des_write_save(const char *path, const des_mesh_view *m, const de
     bin.write(bcflag, N, "bcflag");
     return bin.close();
 }
+
+// Output::write_checkpoint (output.cxx:270-296) for a model without marker
+// sets in 3D: time and compensation pressure, segments, segment flags and
+// volume_old.
+extern "C" int des_write_checkpoint(const char *path, const des_mesh_view *m, double time,
+                                    double compensation_pressure, const double *volume_old)
+{
+    if (!path || !m || !volume_old || (m->nseg > 0 && (!m->segment || !m->segflag))) return DES_ERR_ARG;
+    SaveFile bin(path);
+    if (!bin.ok()) return DES_ERR_ARG;
+    const double tc[2] = {time, compensation_pressure};
+    bin.write(tc, 2, "time compensation_pressure");
+    bin.write(m->segment, 3 * (std::size_t)m->nseg, "segment");
+    bin.write(m->segflag, (std::size_t)m->nseg, "segflag");
+    bin.write(volume_old, (std::size_t)m->nelem, "volume_old");
+    return bin.close();
+}

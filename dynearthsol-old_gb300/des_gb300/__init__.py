@@ -82,6 +82,7 @@ def lib():
     L.des_gpu_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
     L.des_write_save.argtypes = [C.c_char_p, P(abi.MeshView), P(abi.Params), P(C.c_uint),
                                  P(abi.StateView), P(abi.SaveAverages)]
+    L.des_write_checkpoint.argtypes = [C.c_char_p, P(abi.MeshView), C.c_double, C.c_double, P(C.c_double)]
     L.des_gpu_set_averaging.argtypes = [C.c_void_p, C.c_int]
     L.des_gpu_output_snapshot.argtypes = [C.c_void_p, C.c_uint]
     L.des_gpu_output_fetch.argtypes = [C.c_void_p, P(abi.StateView)]
@@ -293,6 +294,13 @@ def write_save(path, mesh, params, bcflag, state, averages=None):
     b = np.ascontiguousarray(bcflag, dtype=np.uint32)
     _ck(lib().des_write_save(str(path).encode(), C.byref(mv), C.byref(params), abi.uptr(b), C.byref(v),
                              C.byref(averages) if averages is not None else None), "des_write_save")
+
+
+def write_checkpoint(path, mesh, state, compensation_pressure):
+    """The .chkpt file of a frame (des_write_checkpoint)."""
+    mv = mesh.view()
+    _ck(lib().des_write_checkpoint(str(path).encode(), C.byref(mv), state.time, compensation_pressure,
+                                   abi.dptr(state.volume_old)), "des_write_checkpoint")
 
 
 def pin(state):

@@ -340,6 +340,11 @@ int  des_gpu_output_snapshot(des_gpu *g, unsigned mask);
 int  des_gpu_output_fetch(des_gpu *g, des_state_view *host);
 int  des_gpu_output_wait(des_gpu *g, des_state_view *host);
 
+/* Writes the .chkpt file of a frame as Output::write_checkpoint
+ * (output.cxx:270-296) does for a 3D model without marker sets.  Host-only. */
+int  des_write_checkpoint(const char *path, const des_mesh_view *mesh, double time,
+                          double compensation_pressure, const double *volume_old);
+
 /* Output::average_fields on the device after every step from the next
  * des_gpu_step on (interval = mesh.quality_check_step_interval; 0 stops it). */
 int  des_gpu_set_averaging(des_gpu *g, int interval);

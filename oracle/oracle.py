@@ -225,6 +225,7 @@ class RefOracle(_Base):
             L.dsr_dsyevh3.argtypes = [P(C.c_double)] * 3
             L.dsr_output_begin.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]
             L.dsr_output_write.argtypes = [C.c_void_p, C.c_int]
+            L.dsr_output_checkpoint.argtypes = [C.c_void_p]
             L.dsr_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
             L.dsr_worst_elem_quality.argtypes = [C.c_void_p, P(C.c_int)]
             L.dsr_worst_elem_quality.restype = C.c_double
@@ -302,6 +303,15 @@ class RefOracle(_Base):
         rc = self.L.dsr_output_write(self.h, int(exact))
         if rc:
             raise RuntimeError("output not set up")
+
+    def output_checkpoint(self, state):
+        """Output::write_checkpoint of `state`: <modelname>.chkpt.<frame>."""
+        self._in(state)
+        if self.L.dsr_output_checkpoint(self.h):
+            raise RuntimeError("output not set up")
+
+    def compensation_pressure(self):
+        return self.L.dsr_compensation_pressure(self.h)
 
     def elem_quality(self, state):
         """The reference's elem_quality of every element, and its

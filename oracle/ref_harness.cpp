@@ -425,6 +425,14 @@ int dsr_output_begin(dsr *h, const char *modelname, int frame, int averaged, int
     h->out = new Output(h->param, 0.0, frame);
     return 0;
 }
+// Output::write_checkpoint of the current state: <modelname>.chkpt.<frame>
+int dsr_output_checkpoint(dsr *h)
+{
+    if (!h->out) return 1;
+    h->out->write_checkpoint(h->param, h->var);
+    return 0;
+}
+
 // Output::write (or write_exact) of the current state: <modelname>.save.<frame>
 int dsr_output_write(dsr *h, int exact)
 {

@@ -72,3 +72,14 @@ def test_save_header_and_layout(tmp_path):
     pos = {h.split("\t")[0]: int(h.split("\t")[1]) for h in head[1:]}
     stress = np.frombuffer(raw[pos["stress"]:pos["density"]], dtype=np.float64).reshape(-1, 6)
     assert np.array_equal(stress, s.stress)
+
+
+@needs_ref
+def test_checkpoint_file_matches_the_reference(tmp_path):
+    c = Case(W.CONFIGS["1"])
+    s = run(c, c.initial_state(), 12)
+    r = RefOracle(c.mesh, c.params)
+    r.output_begin(tmp_path / "ref", frame=1, averaged=False, interval=10)
+    r.output_checkpoint(s)
+    D.write_checkpoint(tmp_path / "ours.chkpt", c.mesh, s, r.compensation_pressure())
+    assert (tmp_path / "ref.chkpt.000001").read_bytes() == (tmp_path / "ours.chkpt").read_bytes()
