@@ -50,6 +50,9 @@ struct MatTable {
     double phi_w, tphi_w, anphi_w, sqanphi_w;
     double psi_w, anpsi_w;
     double visc_min, visc_max, tension_max;
+    // FP32 copies for the quick elastic bound (quick_elastic)
+    float pls0f[kMaxMat], pls1f[kMaxMat], c0f[kMaxMat], c1f[kMaxMat], f0f[kMaxMat], f1f[kMaxMat];
+    float phi_cf, anphi_cf, sqanphi_cf, tphi_cf, phi_wf, anphi_wf, sqanphi_wf, tphi_wf, tension_maxf;
     Mix    mix[kMaxMix];
 };
 
@@ -452,13 +455,70 @@ __device__ __forceinline__ bool surely_elastic(const double *s, double anphi, do
     return fs_lo > margin && ft_hi < -margin;
 }
 
+// The same bound in FP32 from FP32 plastic properties, before any FP64 work on
+// the element: where it holds, the element's stress is the trial and its
+// plastic properties are never needed.  The margin (1e-4 of the stress scale
+// times 1 + anphi) covers the FP32 rounding of the stress, of the properties
+// and of the bound many times over.
+__device__ __forceinline__ bool quick_elastic(const MatTable &M, const Mix &x, double pls, const double *s)
+{
+    const float pl = (float)pls;
+    float c = 0.f, f = 0.f;
+    int n = 0;
+    for (int m = 0; m < M.nmat; ++m) {
+        const int k = x.count[m];
+        if (k == 0) continue;
+        n += k;
+        float cm, fm;
+        if (pl < M.pls0f[m]) {
+            cm = M.c0f[m];
+            fm = M.f0f[m];
+        } else if (pl < M.pls1f[m]) {
+            const float q = (pl - M.pls0f[m]) / (M.pls1f[m] - M.pls0f[m]);
+            cm = M.c0f[m] + q * (M.c1f[m] - M.c0f[m]);
+            fm = M.f0f[m] + q * (M.f1f[m] - M.f0f[m]);
+        } else {
+            cm = M.c1f[m];
+            fm = M.f1f[m];
+        }
+        c += cm * (float)k;
+        f += fm * (float)k;
+    }
+    const float cohesion = c / (float)n, phi = f / (float)n;
+    float anphi, sq, tph;
+    if (phi == M.phi_cf) {
+        anphi = M.anphi_cf;
+        sq = M.sqanphi_cf;
+        tph = M.tphi_cf;
+    } else if (phi == M.phi_wf) {
+        anphi = M.anphi_wf;
+        sq = M.sqanphi_wf;
+        tph = M.tphi_wf;
+    } else {
+        const float sp = sinf(phi * (float)kDeg2Rad);
+        anphi = (1.f + sp) / (1.f - sp);
+        sq = sqrtf(anphi);
+        tph = tanf(phi * (float)kDeg2Rad);
+    }
+    const float amc = 2.f * cohesion * sq;
+    const float ten_max = (phi == 0.f) ? M.tension_maxf : fminf(M.tension_maxf, cohesion / tph);
+    float sf[6];
+    for (int i = 0; i < 6; ++i) sf[i] = (float)s[i];
+    const float mp = (sf[0] + sf[1] + sf[2]) * (1.f / 3.f);
+    const float a = sf[0] - mp, b = sf[1] - mp, cc = sf[2] - mp;
+    const float dev2 = a * a + b * b + cc * cc + 2.f * (sf[3] * sf[3] + sf[4] * sf[4] + sf[5] * sf[5]);
+    const float R = sqrtf(dev2 * (2.f / 3.f)) * (1.f + 1e-5f);
+    const float margin = 1e-4f * (fabsf(mp) + R) * (1.f + anphi) + 1e-30f;
+    return ((mp - R) - anphi * (mp + R) + amc) > margin && ((mp + R) - ten_max) < -margin;
+}
+
+// The return map of elasto_plastic (rheology.cxx:154-302) from the trial s;
 // returns 1 when the principal stresses were computed (+2 when QL was used,
 // +4 when QL failed to converge, +16 for a shear return, +32 for a tensile one)
-__device__ __forceinline__ int elasto_plastic(double bulkm, double shearm, double amc, double anphi,
-                                              double anpsi, double hardn, double ten_max,
-                                              const double *de, double &depls, double *s)
+__device__ __forceinline__ int plastic_return(double bulkm, double shearm, double amc, double anphi,
+                                              double anpsi, double hardn, double ten_max, double &depls,
+                                              double *s)
 {
-    elastic(bulkm, shearm, de, s);
     depls = 0;
     if (surely_elastic(s, anphi, amc, ten_max)) return 0;
     double p[3];
@@ -505,6 +565,15 @@ __device__ __forceinline__ int elasto_plastic(double bulkm, double shearm, doubl
     s[4] = ss02;
     s[5] = ss12;
     return flags;
+}
+
+// elasto_plastic (rheology.cxx:154-302): elastic trial, then the return map
+__device__ __forceinline__ int elasto_plastic(double bulkm, double shearm, double amc, double anphi,
+                                              double anpsi, double hardn, double ten_max,
+                                              const double *de, double &depls, double *s)
+{
+    elastic(bulkm, shearm, de, s);
+    return plastic_return(bulkm, shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
 }
 
 // ---- geometry -------------------------------------------------------------

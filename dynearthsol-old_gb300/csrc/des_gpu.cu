@@ -185,9 +185,26 @@ int build_consts(des_gpu *g)
     M.psi_w = M.d1[0];
     double spsi_w = std::sin(M.psi_w * deg2rad);
     M.anpsi_w = (1 + spsi_w) / (1 - spsi_w);
+    for (int m = 0; m < g->nmat; ++m) {
+        M.pls0f[m] = (float)M.pls0[m];
+        M.pls1f[m] = (float)M.pls1[m];
+        M.c0f[m] = (float)M.c0[m];
+        M.c1f[m] = (float)M.c1[m];
+        M.f0f[m] = (float)M.f0[m];
+        M.f1f[m] = (float)M.f1[m];
+    }
+    M.phi_cf = (float)M.phi_c;
+    M.anphi_cf = (float)M.anphi_c;
+    M.sqanphi_cf = (float)M.sqanphi_c;
+    M.tphi_cf = (float)M.tphi_c;
+    M.phi_wf = (float)M.phi_w;
+    M.anphi_wf = (float)M.anphi_w;
+    M.sqanphi_wf = (float)M.sqanphi_w;
+    M.tphi_wf = (float)M.tphi_w;
     M.visc_min = p.visc_min;
     M.visc_max = p.visc_max;
     M.tension_max = p.tension_max;
+    M.tension_maxf = (float)p.tension_max;
     double pseudo_speed = p.max_vbc_val * p.inertial_scaling;
     for (int i = 0; i < M.nmix; ++i) {
         const std::vector<int> &cnt = g->mix_counts[i];

@@ -163,9 +163,12 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
     } break;
     case 5: { // elasto-plastic
         double depls = 0;
-        double amc, anphi, anpsi, hardn, ten_max;
-        plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
-        flags = elasto_plastic(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, s);
+        elastic(x.bulkm, x.shearm, de, s);
+        if (!quick_elastic(M, x, pls, s)) {
+            double amc, anphi, anpsi, hardn, ten_max;
+            plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
+            flags = plastic_return(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
+        }
         pls += depls;
         dpls = depls;
     } break;
@@ -179,11 +182,14 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
         for (int i = 0; i < 6; ++i) sv[i] = s[i];
         maxwell(x.bulkm, x.shearm, viscosity, dt, dv, de, sv);
         double svII = second_invariant2(sv);
-        double amc, anphi, anpsi, hardn, ten_max;
-        plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
         double sp[6];
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
-        flags = elasto_plastic(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, de, depls, sp);
+        elastic(x.bulkm, x.shearm, de, sp);
+        if (!quick_elastic(M, x, pls, sp)) {
+            double amc, anphi, anpsi, hardn, ten_max;
+            plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
+            flags = plastic_return(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp);
+        }
         double spII = second_invariant2(sp);
         if (svII < spII) {
             for (int i = 0; i < 6; ++i) s[i] = sv[i];
