@@ -182,17 +182,19 @@ def e2e_rate(dev, mesh, steps, barrier, world):
     return world * mesh.nelem * steps / e2e_s, h2d, io_bytes
 
 
-def train_closure(base, local):
-    """The closure for base's material: 300 FP64 steps of a 24x24x8 box of it
-    logged, then 20 epochs of Adam on the GPU."""
+def train_closure(base, local, box=(60, 60, 12), nsteps=300, epochs=20):
+    """The closure for base's material: nsteps FP64 steps of a smaller box of
+    it logged (at most 4M returns kept), then Adam on the GPU."""
     from des_gb300 import abi, closure, workload as W
     t0 = time.perf_counter()
-    dv, tmesh, tp = _fresh_form(W.scaled(base, 24, 24, 8), abi.PREC_FP64, local)
-    rec, nrec = dv.log_returns(300, 4_000_000)
+    dv, tmesh, tp = _fresh_form(W.scaled(base, *box), abi.PREC_FP64, local)
+    rec = closure.collect(dv, nsteps, every=5)
+    nrec = len(rec)
     dv.close()
-    net, trace = closure.fit(rec, tp, epochs=20, seed=1)
+    net, trace = closure.fit(rec, tp, epochs=epochs, seed=1)
     net.tol = 1e-3
-    info = {"records": int(nrec), "box": f"24x24x8 x6 = {tmesh.nelem} tets, 300 FP64 steps",
+    info = {"records": int(nrec), "kept": int(len(rec)),
+            "box": f"{box[0]}x{box[1]}x{box[2]} x6 = {tmesh.nelem} tets, {nsteps} FP64 steps",
             "seconds": time.perf_counter() - t0, "loss_first": float(trace[:100].mean()),
             "loss_last": float(trace[-100:].mean()), "tol": net.tol}
     return net, info
@@ -242,7 +244,7 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     out = {"workload": f"{cfg.name}: weak Mohr-Coulomb material yielding from a weak-seed "
                        "row (1-4% of the elements return each step over the timed steps)",
            "closure_training": training}
-    warm = max(args.warmup, 20)
+    warm = max(args.warmup, 100)      # let the yielding spread from the weak row
     prof = max(2, min(args.steps, 5))
     names = ["N-A", "E-B", "N-B", "E-C", "N-C", "E-A"]
     d64 = S = None

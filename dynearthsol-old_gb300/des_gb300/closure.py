@@ -145,6 +145,21 @@ def rebuild(y, trial):
     return y[:, 0:1] * np.array([1, 1, 1, 0, 0, 0]) + (y[:, 1] / D)[:, None] * n + (y[:, 2] / D)[:, None] * q
 
 
+def collect(device, nsteps, every=10, capacity=4_000_000):
+    """Training records from an FP64 device: the returns of one step in every
+    `every` over nsteps steps (the others run without logging), at most
+    `capacity` in all, so that the data span the run rather than its start."""
+    parts, kept = [], 0
+    per = max(1, capacity // max(1, nsteps // every))
+    for _ in range(nsteps // every):
+        rec, _ = device.log_returns(1, per)
+        parts.append(rec)
+        kept += len(rec)
+        if every > 1:
+            device.step(every - 1)
+    return np.concatenate(parts) if parts else np.zeros((0, abi.RET_RECORD), np.float32)
+
+
 def dataset(rec, params):
     """(raw inputs, targets) of the usable records."""
     bulkm, shearm, pls_sat = single_material(params)
