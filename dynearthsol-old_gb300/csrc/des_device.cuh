@@ -400,25 +400,6 @@ __device__ __forceinline__ int principal3(const double *s, double p[3], double v
     return rc;
 }
 
-// ---- division by the constants 3 and 6 ------------------------------------
-// x / d rounded as the IEEE division: q = x * RN(1/d) corrected by one fused
-// multiply-add, q + (x - q d) RN(1/d) (Markstein's correction for a constant
-// divisor, "Computation of elementary functions on the IBM RISC System/6000",
-// 1990).  For d = 3 and 6 the corrected quotient equals the correctly rounded
-// one for every x of moderate exponent (checked on 2e9 seeded operands each,
-// tie patterns included); zeros, subnormals and extreme exponents take the
-// division.  Three FP64 operations in place of the division's longer sequence.
-__device__ __forceinline__ double div_const(double x, double d, double r)
-{
-    const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu;
-    if (e < 64u || e > 1983u) return x / d;
-    const double q = x * r;
-    return fma(fma(-q, d, x), r, q);
-}
-__device__ __forceinline__ double div3(double x) { return div_const(x, 3.0, 1.0 / 3.0); }
-__device__ __forceinline__ double div6(double x) { return div_const(x, 6.0, 1.0 / 6.0); }
-__device__ __forceinline__ float div3(float x) { return x / 3.f; }
-
 // ---- rheology (rheology.cxx:108-302, 3D) ----------------------------------
 
 template <class R>
@@ -436,8 +417,8 @@ __device__ __forceinline__ void maxwell(R bulkm, R shearm, R viscosity, R dt, R 
     R tmp = R(0.5) * dt * shearm / viscosity;
     R f1 = 1 - tmp;
     R f2 = 1 / (1 + tmp);
-    R dev = div3(tr3(de));
-    R s0 = div3(tr3(s));
+    R dev = tr3(de) / 3;
+    R s0 = tr3(s) / 3;
     for (int i = 0; i < 3; ++i)
         s[i] = ((s[i] - s0) * f1 + 2 * shearm * (de[i] - dev)) * f2 + s0 + bulkm * dv;
     for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + 2 * shearm * de[i]) * f2;
@@ -446,7 +427,7 @@ __device__ __forceinline__ void maxwell(R bulkm, R shearm, R viscosity, R dt, R 
 template <class R>
 __device__ __forceinline__ void viscous(R bulkm, R viscosity, R total_dv, const R *edot, R *s)
 {
-    R dev = div3(tr3(edot));
+    R dev = tr3(edot) / 3;
     for (int i = 0; i < 3; ++i) s[i] = 2 * viscosity * (edot[i] - dev) + bulkm * total_dv;
     for (int i = 3; i < 6; ++i) s[i] = 2 * viscosity * edot[i];
 }
@@ -610,8 +591,8 @@ __device__ __forceinline__ double tet_volume(const double *d0, const double *d1,
     double z01 = d0[2] - d1[2];
     double z12 = d1[2] - d2[2];
     double z23 = d2[2] - d3[2];
-    return div6(x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) +
-                x23 * (y12 * z01 - y01 * z12));
+    return (x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) +
+            x23 * (y12 * z01 - y01 * z12)) / 6;
 }
 
 // geometry.cxx:53-83 (3D)

@@ -138,7 +138,7 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
     double old_s = tr3(s);
     {
         double div = tr3(edot);
-        for (int i = 0; i < 3; ++i) edot[i] += div3(edv - div);
+        for (int i = 0; i < 3; ++i) edot[i] += (edv - div) / 3;
     }
     for (int i = 0; i < 6; ++i) es[i] += edot[i] * dt;
     double de[6];
@@ -558,7 +558,7 @@ __global__ void k_nmd_apply(Dev d)
     double dpe = 0;
     for (int i = 0; i < 4; ++i) dpe += a[i];
     double dp_el = dpe / 4;
-    double ddp = div3(-d.dp[e] + dp_el);
+    double ddp = (-d.dp[e] + dp_el) / 3;
     for (int i = 0; i < 3; ++i) d.stress[i * E + e] += ddp;
 }
 
@@ -940,7 +940,7 @@ __global__ void k_fe_c(Dev d)
     double dpe = 0;
     for (int i = 0; i < 4; ++i) dpe += a[i];
     double dp_el = dpe / 4;
-    double ddp = div3(-d.dp[e] + dp_el);
+    double ddp = (-d.dp[e] + dp_el) / 3;
     double s[6];
     load6(d.stress, E, e, s);
     for (int i = 0; i < 3; ++i) s[i] += ddp;
