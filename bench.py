@@ -301,6 +301,35 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     return out
 
 
+def large_case_forms(args, local, world, reduce):
+    """Config 5 (400x400x80 hexes x 6 = 76.8M tets, three material layers,
+    elasto-visco-plastic): both forms, their device footprint and rate."""
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+    cfg = W.CONFIGS["5"]
+    t0 = time.perf_counter()
+    mesh, p, T, pls, topo = D.setup_case(cfg)
+    s0 = W.new_state(mesh, T, pls)
+    out = {"workload": f"{cfg.name}: {mesh.nelem} tets / {mesh.nnode} nodes, 3 layers, "
+                       "elasto-visco-plastic", "host_setup_s": time.perf_counter() - t0}
+    k = max(3, min(args.steps, 10))
+    for name, prec in (("fp64_plain", abi.PREC_FP64), ("fp32_mixed", abi.PREC_FP32)):
+        q = abi.Params.from_buffer_copy(p)
+        q.precision = prec
+        dv = D.Device(mesh, q, device=local)
+        dv.upload(s0, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dv.init_fields()
+        dv.step(3)
+        ms = dv.time_steps(k)
+        v, ms = replica_throughput(ms, mesh.nelem, k, world, reduce)
+        rep = dv.report()
+        out[name] = {"value": v, "ms_per_step": ms / k, "steps": k, "device_gb": dv.device_bytes / 1e9,
+                     "status": rep.status}
+        dv.close()
+    out["fp32_mixed"]["speedup_vs_fp64"] = out["fp32_mixed"]["value"] / out["fp64_plain"]["value"]
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -406,6 +435,9 @@ def run_ours(args):
     if not args.no_yielding:
         forms["yielding"] = yielding_forms(args, local, world, barrier,
                                            torch_reduce_max(f"cuda:{local}") if dist else None, compare)
+    if not args.no_large:
+        forms["config5"] = large_case_forms(args, local, world,
+                                            torch_reduce_max(f"cuda:{local}") if dist else None)
 
     # per-pass device times over extra steps (same arithmetic, launched one by one)
     prof_steps = max(2, min(args.steps, 5))
@@ -522,6 +554,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-yielding", action="store_true",
                     help="skip the forms on the yielding workload")
+    ap.add_argument("--no-large", action="store_true", help="skip config 5 (76.8M tets)")
     ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure"], default=None,
                     help="run one form alone on --config/--box (for profiling)")
     ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
