@@ -479,21 +479,23 @@ def run_ours(args):
     dev.output_fetch(out_host)
     dev.output_wait(out_host)                  # warm-up
     dev.report()
-    t0 = time.perf_counter()
-    dev.step(5)
-    t_plain = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    dev.output_snapshot()
-    dev.output_fetch(out_host)
-    dev.step(5)
-    dev.output_wait(out_host)
-    dev.report()
-    t_overlap = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    dev.output_snapshot()
-    dev.output_fetch(out_host)
-    dev.output_wait(out_host)
-    t_alone = time.perf_counter() - t0
+    t_plain = t_overlap = t_alone = float("inf")
+    for _ in range(3):                          # the best of three of each
+        t0 = time.perf_counter()
+        dev.step(5)
+        t_plain = min(t_plain, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        dev.output_snapshot()
+        dev.output_fetch(out_host)
+        dev.step(5)
+        dev.output_wait(out_host)
+        dev.report()
+        t_overlap = min(t_overlap, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        dev.output_snapshot()
+        dev.output_fetch(out_host)
+        dev.output_wait(out_host)
+        t_alone = min(t_alone, time.perf_counter() - t0)
     D.unpin(out_host)
     output = {"bytes": out_bytes, "download_alone_ms": t_alone * 1e3,
               "five_steps_ms": t_plain * 1e3, "five_steps_with_download_ms": t_overlap * 1e3}
