@@ -28,24 +28,6 @@
 
 namespace des {
 
-// double -> float rounded to nearest even from the bits, on the integer pipes
-// (the same result as the conversion instruction, which runs on the FP64 pipe
-// that bounds the FP32 form's geometry); outside the float-normal range the
-// conversion itself is used
-__device__ __forceinline__ float d2f(double x)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    if ((b << 1) == 0) return __uint_as_float(hi);     // +-0
-    const unsigned ex = (hi >> 20) & 0x7ffu;
-    if (ex - 897u > 253u) return (float)x;
-    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned rem = lo & 0x1fffffffu;
-    unsigned f = (hi & 0x80000000u) | ((ex - 896u) << 23) | m;
-    f += (rem > 0x10000000u) || (rem == 0x10000000u && (m & 1u));   // a carry moves into the exponent
-    return __uint_as_float(f);
-}
-
 struct MixF {
     float bulkm, shearm, cp, k, rho_qs;
     float rho_alpha;        // sum_m k_m rho0_m alpha_m / n: thermal part of the density
@@ -133,8 +115,8 @@ __device__ __forceinline__ void f_store6(float *a, size_t E, int e, const float 
 // element mean temperature in FP32 (from the FP64 accumulator)
 __device__ __forceinline__ float f_elem_T(const DevF &d, int4 c)
 {
-    return elem_mean4(d2f(__ldg(d.T + c.x)), d2f(__ldg(d.T + c.y)), d2f(__ldg(d.T + c.z)),
-                      d2f(__ldg(d.T + c.w)));
+    return elem_mean4((float)__ldg(d.T + c.x), (float)__ldg(d.T + c.y), (float)__ldg(d.T + c.z),
+                      (float)__ldg(d.T + c.w));
 }
 
 // matprops.cxx:707-728 in FP32
@@ -343,8 +325,8 @@ __device__ __forceinline__ void f_next_contrib(const DevF &d, int e, int4 c, con
         // conduction vector kv (grad N_i . grad T) with grad T from temperature
         // differences (sum_j grad N_j = 0), differences taken in FP64
         double T0 = __ldg(d.T + c.x);
-        float t1 = d2f(__ldg(d.T + c.y) - T0), t2 = d2f(__ldg(d.T + c.z) - T0),
-              t3 = d2f(__ldg(d.T + c.w) - T0);
+        float t1 = (float)(__ldg(d.T + c.y) - T0), t2 = (float)(__ldg(d.T + c.z) - T0),
+              t3 = (float)(__ldg(d.T + c.w) - T0);
         float gx = dx[1] * t1 + dx[2] * t2 + dx[3] * t3;
         float gy = dy[1] * t1 + dy[2] * t2 + dy[3] * t3;
         float gz = dz[1] * t1 + dz[2] * t2 + dz[3] * t3;
@@ -643,11 +625,11 @@ __device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, doubl
     const double vol = det * (1.0 / 6.0);
     f_reference_force(d, e, cf, vol);
     // the gradients themselves are FP32: c_i / (6 V)
-    const float iv = 1.f / d2f(det);
+    const float iv = 1.f / (float)det;
     for (int i = 0; i < 4; ++i) {
-        dx[i] = d2f(cf[i][0]) * iv;
-        dy[i] = d2f(cf[i][1]) * iv;
-        dz[i] = d2f(cf[i][2]) * iv;
+        dx[i] = (float)cf[i][0] * iv;
+        dy[i] = (float)cf[i][1] * iv;
+        dz[i] = (float)cf[i][2] * iv;
         d.shp[(0 + i) * E + e] = dx[i];
         d.shp[(4 + i) * E + e] = dy[i];
         d.shp[(8 + i) * E + e] = dz[i];
@@ -674,7 +656,7 @@ __global__ void kf_fe_a(DevF d)
         d.vol_old[e] = d.vol[e];
         d.vol[e] = vol;
         if (!(vol > 0)) atomicOr(&d.clk->status, 0x4u);
-        float volf = d2f(vol);
+        float volf = (float)vol;
         d.c_vol[e] = volf;
         const MixF &xf = F.mix[d.mix[e]];
         {
