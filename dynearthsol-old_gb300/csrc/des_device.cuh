@@ -714,6 +714,12 @@ __device__ __forceinline__ double min_height(const double X[4][3], double vol)
     return 3 * vol / maxa;
 }
 
+// true for NaN or +-Inf, from the exponent bits (integer pipes)
+__device__ __forceinline__ bool not_finite(double x)
+{
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) == 0x7ff0000000000000ull;
+}
+
 // orderable 64-bit image of a double (total order for non-NaN values)
 __device__ __forceinline__ unsigned long long order_bits(double x)
 {

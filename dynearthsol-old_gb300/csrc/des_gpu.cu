@@ -561,7 +561,7 @@ const char *des_gpu_error_string(int code)
     case DES_ERR_NOMEM: return "device allocation failed";
     case DES_ERR_UNSUPPORTED: return "option not supported by this library";
     case DES_ERR_SIZE: return "size above the entry point's limit";
-    case DES_ERR_DT: return "dt <= 0";
+    case DES_ERR_DT: return "dt <= 0 or non-finite coordinates";
     case DES_ERR_TOPOLOGY: return "inconsistent mesh topology";
     default: return "unknown error";
     }
@@ -1294,7 +1294,9 @@ int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)
     if (!report) return DES_OK;
     int rc = des_gpu_report(g, report);
     if (rc) return rc;
-    if (report->status & DES_STATUS_DT_NONPOSITIVE) return DES_ERR_DT;
+    // the reference stops with exit code 11 on both (geometry.cxx:321-325,
+    // output.cxx:195-208)
+    if (report->status & (DES_STATUS_DT_NONPOSITIVE | DES_STATUS_NONFINITE)) return DES_ERR_DT;
     return DES_OK;
 }
 

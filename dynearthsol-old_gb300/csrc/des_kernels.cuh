@@ -654,6 +654,8 @@ __global__ void k_coord(Dev d)
     d.x[n] += d.vx[n] * dt;
     d.y[n] += d.vy[n] * dt;
     d.z[n] += d.vz[n] * dt;
+    // output.cxx:195-208 stops on NaN/Inf coordinates
+    if (not_finite(d.x[n]) || not_finite(d.y[n]) || not_finite(d.z[n])) atomicOr(&d.clk->status, 0x2u);
 }
 
 // geometry.cxx:94-110; save_old copies volume into volume_old first
@@ -972,9 +974,12 @@ __global__ void k_fn_c(Dev d)
     d.vx[n] = v[0];
     d.vy[n] = v[1];
     d.vz[n] = v[2];
-    d.x[n] += v[0] * dt;
-    d.y[n] += v[1] * dt;
-    d.z[n] += v[2] * dt;
+    const double x = d.x[n] + v[0] * dt, y = d.y[n] + v[1] * dt, z = d.z[n] + v[2] * dt;
+    d.x[n] = x;
+    d.y[n] = y;
+    d.z[n] = z;
+    // output.cxx:195-208 stops on NaN/Inf coordinates
+    if (not_finite(x) || not_finite(y) || not_finite(z)) atomicOr(&d.clk->status, 0x2u);
 }
 
 // E-A: update_mesh element half, rotate_stress, next-step contributions, dt

@@ -608,9 +608,12 @@ __global__ void kf_fn_c(DevF d)
     d.vx[n] = v[0];
     d.vy[n] = v[1];
     d.vz[n] = v[2];
-    d.x[n] += (double)v[0] * dt;
-    d.y[n] += (double)v[1] * dt;
-    d.z[n] += (double)v[2] * dt;
+    const double x = d.x[n] + (double)v[0] * dt, y = d.y[n] + (double)v[1] * dt,
+                 z = d.z[n] + (double)v[2] * dt;
+    d.x[n] = x;
+    d.y[n] = y;
+    d.z[n] = z;
+    if (not_finite(x) || not_finite(y) || not_finite(z)) atomicOr(&d.clk->status, 0x2u);
 }
 
 // FP64 volume and shape derivatives of one element, rounded to FP32 for use;

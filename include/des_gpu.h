@@ -35,7 +35,7 @@ extern "C" {
 #define DES_ERR_NOMEM       4   /* device allocation failed */
 #define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / surface processes / fp32 closure not built */
 #define DES_ERR_SIZE        6   /* size above a fixed limit of the entry point */
-#define DES_ERR_DT         11   /* compute_dt produced dt <= 0 (geometry.cxx:321-325) */
+#define DES_ERR_DT         11   /* dt <= 0 (geometry.cxx:321-325) or NaN/Inf coordinates (output.cxx:195-208) */
 #define DES_ERR_TOPOLOGY   12   /* a segment is on no element (mesh.cxx:1676-1678) */
 
 /* status bits reported by des_gpu_step (device-side status word) */

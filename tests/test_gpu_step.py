@@ -147,3 +147,21 @@ def test_page_locked_host_buffers(gpu, precision):
         dev.close()
         out.append(b)
     assert not diff_fields(out[0], out[1], COMPARED)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_FP32])
+def test_nonfinite_coordinates_stop_the_step(gpu, precision):
+    """A NaN velocity reaches the coordinates; the step reports it with the
+    reference's exit code 11 (output.cxx:195-208) instead of running on."""
+    c = case("tiny")
+    s = c.state_after(2)
+    s.vel[3, 1] = np.nan
+    p = abi.Params.from_buffer_copy(c.params)
+    p.precision = precision
+    dev = D.Device(c.mesh, p, device=0)
+    dev.upload(s, abi.F_ALL)
+    with pytest.raises(RuntimeError, match="error 11"):
+        dev.step(1)
+    assert dev.report().status & abi.DES_STATUS_NONFINITE
+    dev.close()
