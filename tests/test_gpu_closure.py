@@ -243,3 +243,43 @@ def test_closure_error_is_within_the_loops_own_sensitivity():
         got = rel_l2(getattr(c, f), getattr(a, f))
         assert own > 1e-4, (f, own)             # the instability this bar stands on
         assert got <= 3 * own, (f, got, own)
+
+
+def evp_yield_config(nx=12, ny=12, nz=6):
+    """The yielding box with the elasto-visco-plastic rheology: where the
+    Mohr-Coulomb return gives the smaller second invariant the plastic stress
+    is taken (rheology.cxx:628-638)."""
+    c = plastic_config(nx, ny, nz)
+    d = dict(c.__dict__)
+    d["rheology"] = "evp"
+    d["name"] = c.name + "_evp"
+    return W.Config(**d)
+
+
+def test_evp_closure_rejecting_everything_is_the_exact_pass():
+    cfg = evp_yield_config()
+    d64, mesh, p = fresh(cfg, abi.PREC_FP64)
+    rec = closure.collect(d64, 150, every=3)
+    s64 = download(d64, mesh)
+    d64.close()
+    assert len(rec) > 1000
+    net, _ = closure.fit(rec, p, epochs=15, seed=3)
+    blank = abi.Mlp.from_buffer_copy(net)
+    blank.arr("env_lo")[:] = 1.0
+    blank.arr("env_hi")[:] = -1.0
+    out = {}
+    for name, use in (("none", None), ("blank", blank), ("net", net)):
+        dv, _, _ = fresh(cfg, abi.PREC_FP32, s64)
+        if use is not None:
+            dv.set_closure(use)
+        out[name] = (dv.step(5), download(dv, mesh))
+        dv.close()
+    rb, sb = out["blank"]
+    rn, sn = out["none"]
+    assert rb.closure_candidates == 0 and rb.exact_returns > 0
+    for f in ("stress", "strain", "plstrain", "vel"):
+        assert np.array_equal(getattr(sb, f), getattr(sn, f)), f
+    r, s = out["net"]
+    assert r.closure_accepted > 0
+    # five steps from the same state: within the one-step bar of the EP test, five times
+    assert rel_l2(s.stress, sn.stress) < 5 * 3e-3
