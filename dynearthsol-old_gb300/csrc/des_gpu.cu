@@ -137,6 +137,48 @@ int check_params(const des_params &p, int nmat)
     return DES_OK;
 }
 
+// The distinct marker-count vectors ("mixes") of elemmarkers [nelem][nmat]
+// in order of first appearance, and the element -> mix map.  Every material
+// property MatProps derives from an element's counts (matprops.cxx:193-331)
+// is a function of its mix.
+int build_mix(const int *elemmarkers, int nelem, int nmat, std::vector<std::vector<int>> &counts,
+              std::vector<unsigned char> &mix)
+{
+    counts.clear();
+    mix.assign((size_t)nelem, 0);
+    std::map<std::vector<int>, int> ids;
+    std::vector<int> prev, cur((size_t)nmat);
+    int prev_id = -1;
+    for (int e = 0; e < nelem; ++e) {
+        const int *c = elemmarkers + (size_t)nmat * e;
+        cur.assign(c, c + nmat);
+        int n = 0;
+        for (int k = 0; k < nmat; ++k) {
+            if (cur[k] < 0) return DES_ERR_TOPOLOGY;
+            n += cur[k];
+        }
+        if (n <= 0) return DES_ERR_TOPOLOGY;   // MarkerSet rejects an element without markers
+        if (prev_id >= 0 && cur == prev) {
+            mix[e] = (unsigned char)prev_id;
+            continue;
+        }
+        auto it = ids.find(cur);
+        int id;
+        if (it == ids.end()) {
+            id = (int)ids.size();
+            if (id >= kMaxMix) return DES_ERR_SIZE;
+            ids[cur] = id;
+            counts.push_back(cur);
+        } else {
+            id = it->second;
+        }
+        mix[e] = (unsigned char)id;
+        prev = cur;
+        prev_id = id;
+    }
+    return DES_OK;
+}
+
 // Consts from params and the distinct marker-count vectors
 int build_consts(des_gpu *g)
 {
@@ -592,44 +634,11 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     g->nmat = m->nmat;
     for (int i = 0; i < DES_NBDRY; ++i) g->bfacets_count[i] = topo->bfacets_count[i];
 
-    // distinct marker-count vectors ("mixes") and the element -> mix map
-    std::vector<unsigned char> mix(m->nelem);
-    {
-        std::map<std::vector<int>, int> ids;
-        std::vector<int> prev, cur(m->nmat);
-        int prev_id = -1;
-        for (int e = 0; e < m->nelem; ++e) {
-            const int *c = m->elemmarkers + (size_t)m->nmat * e;
-            cur.assign(c, c + m->nmat);
-            int n = 0;
-            for (int k = 0; k < m->nmat; ++k) n += cur[k];
-            if (n <= 0) {
-                des_topology_free(topo);
-                delete g;
-                return DES_ERR_TOPOLOGY;   // MarkerSet rejects an element without markers
-            }
-            if (prev_id >= 0 && cur == prev) {
-                mix[e] = (unsigned char)prev_id;
-                continue;
-            }
-            auto it = ids.find(cur);
-            int id;
-            if (it == ids.end()) {
-                id = (int)ids.size();
-                if (id >= kMaxMix) {
-                    des_topology_free(topo);
-                    delete g;
-                    return DES_ERR_SIZE;
-                }
-                ids[cur] = id;
-                g->mix_counts.push_back(cur);
-            } else {
-                id = it->second;
-            }
-            mix[e] = (unsigned char)id;
-            prev = cur;
-            prev_id = id;
-        }
+    std::vector<unsigned char> mix;
+    if ((rc = build_mix(m->elemmarkers, m->nelem, m->nmat, g->mix_counts, mix))) {
+        des_topology_free(topo);
+        delete g;
+        return rc;
     }
 
     auto fail = [&](int code) {
@@ -776,6 +785,26 @@ int des_gpu_set_params(des_gpu *g, const des_params *p)
         g->graph = nullptr;
         if (g->hF.rheol != 5 && g->hF.rheol != 7) g->closure = false;
     }
+    return DES_OK;
+}
+
+int des_gpu_set_elemmarkers(des_gpu *g, const int *elemmarkers)
+{
+    if (!g || !elemmarkers) return DES_ERR_ARG;
+    std::vector<std::vector<int>> counts;
+    std::vector<unsigned char> mix;
+    int rc = build_mix(elemmarkers, g->nelem, g->nmat, counts, mix);
+    if (rc) return rc;
+    // the network was trained on one material mix
+    if (g->closure && counts != g->mix_counts) return DES_ERR_UNSUPPORTED;
+    DES_CUDA(cudaMemcpyAsync(const_cast<unsigned char *>(g->d.mix), mix.data(), (size_t)g->nelem,
+                             cudaMemcpyHostToDevice, g->stream));
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    g->mix_counts.swap(counts);
+    if ((rc = build_consts(g))) return rc;
+    // the conduction and (FP32 form) reference-force terms prepared for the
+    // next step depend on the mix
+    g->primed = false;
     return DES_OK;
 }
 
@@ -1418,6 +1447,62 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
     rc = des_gpu_step(g, nsteps, report);
     if (rc) return rc;
     return des_gpu_download(g, host, mask);
+}
+
+// remesh (remeshing.cxx:1963-2067) after the host's new mesh, interpolation
+// and marker remap: a fresh device state for the new mesh takes the handle's
+// place, with the interpolated fields and the handle's clock, closure and
+// averaging settings
+int des_gpu_remesh(des_gpu *g, const des_mesh_view *mesh, const des_state_view *host,
+                   int reset_bottom_coord0)
+{
+    if (!g || !mesh || !host) return DES_ERR_ARG;
+    if (host->nnode != mesh->nnode || host->nelem != mesh->nelem || mesh->nmat != g->nmat) return DES_ERR_ARG;
+    if (!host->coord || !host->coord0 || !host->vel || !host->temperature || !host->plstrain ||
+        !host->delta_plstrain || !host->strain || !host->stress)
+        return DES_ERR_ARG;
+    Clock c;
+    int rc = read_clock(g, c);
+    if (rc) return rc;
+    if (g->copy_stream) DES_CUDA(cudaStreamSynchronize(g->copy_stream));
+    des_gpu *ng = nullptr;
+    if ((rc = des_gpu_create(mesh, &g->P, g->device, &ng))) return rc;
+    auto fail = [&](int code) {
+        des_gpu_destroy(ng);
+        return code;
+    };
+    if (g->closure) {
+        // the network was trained on one material mix
+        if (ng->mix_counts != g->mix_counts) return fail(DES_ERR_UNSUPPORTED);
+        if ((rc = dev_alloc(ng, &ng->dnet, 1))) return fail(rc);
+        if (cudaMemcpy(ng->dnet, g->dnet, sizeof(MlpDev), cudaMemcpyDeviceToDevice) != cudaSuccess)
+            return fail(DES_ERR_CUDA);
+        ng->closure = true;
+    }
+    // averaging restarts with the next step (remeshing falls on an
+    // interval's last step, output.cxx:229-233)
+    if (g->avg_interval > 0 && (rc = des_gpu_set_averaging(ng, g->avg_interval))) return fail(rc);
+    // the fields remesh interpolates (brc-interpolation.cxx:219-242,
+    // nn-interpolation.cxx:290-325); the rest is reallocated (fields.cxx:57-105)
+    const unsigned interpolated = DES_F_COORD | DES_F_COORD0 | DES_F_VEL | DES_F_TEMPERATURE |
+                                  DES_F_PLSTRAIN | DES_F_STRAIN | DES_F_STRESS;
+    if ((rc = des_gpu_upload(ng, host, interpolated))) return fail(rc);
+    if (reset_bottom_coord0) {
+        k_reset_bottom_coord0<<<blocks(ng->nnode, kNodeBlock), kNodeBlock, 0, ng->stream>>>(ng->d,
+                                                                                       -ng->P.zlength);
+        if (cudaGetLastError() != cudaSuccess) return fail(DES_ERR_CUDA);
+    }
+    k_clock_set<<<1, 32, 0, ng->stream>>>(ng->dclk, c.time, c.dt, c.steps, 1);
+    if (cudaGetLastError() != cudaSuccess) return fail(DES_ERR_CUDA);
+    // compute_volume, volume_old = volume, compute_mass, compute_shape_fn
+    if ((rc = derive_geometry(ng))) return fail(rc);
+    if (cudaMemcpyAsync(ng->d.vol_old, ng->d.vol, sizeof(double) * (size_t)ng->nelem,
+                        cudaMemcpyDeviceToDevice, ng->stream) != cudaSuccess)
+        return fail(DES_ERR_CUDA);
+    if ((rc = finish(ng))) return fail(rc);
+    std::swap(*g, *ng);
+    des_gpu_destroy(ng);
+    return DES_OK;
 }
 
 #define ELEM_GRID(g) blocks((g)->nelem, kElemBlock), kElemBlock, 0, (g)->stream

@@ -632,6 +632,15 @@ __global__ void k_velocity(Dev d)
     d.vz[n] += dt * d.fz[n] / m;
 }
 
+// remeshing.cxx:2046-2054: the bottom nodes' coord0 back on z = -zlength
+// (bnodes[iboundz0] are the nodes flagged on that boundary, mesh.cxx:1553-1566)
+__global__ void k_reset_bottom_coord0(Dev d, double zbottom)
+{
+    int n = gtid();
+    if (n >= d.nnode) return;
+    if (d.bcflag[n] & kBoundZ0) d.z0[n] = zbottom;
+}
+
 __global__ void k_vbcs(Dev d)
 {
     int n = gtid();

@@ -47,6 +47,8 @@ def lib():
     L.des_gpu_create.argtypes = [P(abi.MeshView), P(abi.Params), C.c_int, P(C.c_void_p)]
     L.des_gpu_destroy.argtypes = [C.c_void_p]
     L.des_gpu_set_params.argtypes = [C.c_void_p, P(abi.Params)]
+    L.des_gpu_set_elemmarkers.argtypes = [C.c_void_p, P(C.c_int)]
+    L.des_gpu_remesh.argtypes = [C.c_void_p, P(abi.MeshView), P(abi.StateView), C.c_int]
     L.des_gpu_upload.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
     L.des_gpu_download.argtypes = [C.c_void_p, P(abi.StateView), C.c_uint]
     L.des_gpu_init_fields.argtypes = [C.c_void_p]
@@ -156,6 +158,22 @@ class Device:
     def set_params(self, params):
         self.params = params
         _ck(self.L.des_gpu_set_params(self.h, C.byref(params)), "des_gpu_set_params")
+
+    def set_elemmarkers(self, elemmarkers):
+        """New marker counts [nelem][nmat] for the same mesh (after a phase change)."""
+        em = np.ascontiguousarray(elemmarkers, dtype=np.int32)
+        if em.shape != (self.mesh.nelem, self.mesh.nmat):
+            raise ValueError(f"elemmarkers has shape {em.shape}")
+        _ck(self.L.des_gpu_set_elemmarkers(self.h, abi.iptr(em)), "des_gpu_set_elemmarkers")
+
+    def remesh(self, mesh, state, reset_bottom_coord0=False):
+        """The device half of remesh: `mesh` is the new mesh (with the
+        remapped marker counts), `state` its interpolated fields."""
+        mv = mesh.view()
+        v = state.view()
+        _ck(self.L.des_gpu_remesh(self.h, C.byref(mv), C.byref(v), int(bool(reset_bottom_coord0))),
+            "des_gpu_remesh")
+        self.mesh, self._mv = mesh, mv
 
     def upload(self, state, mask=abi.F_ALL):
         v = state.view()

@@ -215,6 +215,40 @@ int  des_gpu_create(const des_mesh_view *mesh, const des_params *params, int dev
 int  des_gpu_destroy(des_gpu *g);
 int  des_gpu_set_params(des_gpu *g, const des_params *params);
 
+/* New per-element marker counts [nelem][nmat] (mesh->elemmarkers layout) for
+ * the same mesh: the device's material tables follow the counts that
+ * phase_changes (phasechanges.cxx:232-258) or a marker remap leaves in
+ * var.elemmarkers, which MatProps reads through a reference
+ * (matprops.cxx:165).  The reference calls compute_dt right after
+ * phase_changes (dynearthsol.cxx:382-393): call des_gpu_compute_dt after this
+ * at steps % 10 == 0.  Nodal masses stay those of the last update_mesh, as in
+ * the reference; conductivities, densities and moduli of the next step follow
+ * the new counts.  DES_ERR_TOPOLOGY for an element without markers (or a
+ * negative count), DES_ERR_SIZE above 256 distinct count vectors,
+ * DES_ERR_UNSUPPORTED when a closure is set and the counts change; the device
+ * is unchanged after any error. */
+int  des_gpu_set_elemmarkers(des_gpu *g, const int *elemmarkers);
+
+/* The device half of remesh (remeshing.cxx:1963-2067).  The host has built the
+ * new mesh, interpolated the fields and remapped the markers (new_mesh,
+ * nearest_neighbor_interpolation, barycentric_node_interpolation,
+ * remap_markers); mesh is the new mesh (connectivity, segments, segflag and
+ * the remapped elemmarkers), host holds its interpolated fields: coord,
+ * coord0, vel, temperature, plstrain, delta_plstrain, strain and stress.
+ * The handle then holds a device state for the new mesh (support lists,
+ * boundary flags and material tables rebuilt, reallocated fields zero as
+ * reallocate_variables leaves them) and runs what remesh does after
+ * reallocate_variables: compute_volume, volume_old = volume, compute_mass,
+ * compute_shape_fn, and with reset_bottom_coord0 (remeshing_option 1, 2 or
+ * 11) coord0 z = -zlength on the bottom boundary.  time, dt and steps, the
+ * parameters (boundary normals included), the closure and the averaging
+ * interval carry over.  For output during remeshing call
+ * des_gpu_update_strain_rate and des_gpu_update_force after it, as remesh
+ * does.  DES_ERR_UNSUPPORTED when a closure is set and the new mesh's marker
+ * counts differ from the old; after any error the handle is unchanged. */
+int  des_gpu_remesh(des_gpu *g, const des_mesh_view *mesh, const des_state_view *host,
+                    int reset_bottom_coord0);
+
 /* Host Variables -> device (fields in mask).  Marks nodal masses as current,
  * so the next step uses them as the reference does after update_mesh. */
 int  des_gpu_upload(des_gpu *g, const des_state_view *host, unsigned mask);

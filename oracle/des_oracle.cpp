@@ -404,6 +404,16 @@ int dso_set_params(dso *o, const des_params *p)
     return DES_OK;
 }
 
+// MatProps reads var.elemmarkers through a reference (matprops.cxx:165), so
+// the counts phase_changes writes (phasechanges.cxx:248-254) take effect in
+// the next property lookup
+int dso_set_elemmarkers(dso *o, const int *elemmarkers)
+{
+    if (!o || !elemmarkers) return DES_ERR_ARG;
+    o->markers.assign(elemmarkers, elemmarkers + (size_t)o->nmat * o->nelem);
+    return DES_OK;
+}
+
 int dso_create(const des_mesh_view *m, const des_params *p, dso **out)
 {
     if (!m || !p || !out || m->nnode < 1 || m->nelem < 1 || m->nmat < 1) return DES_ERR_ARG;

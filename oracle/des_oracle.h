@@ -22,6 +22,8 @@ typedef struct dso dso;
 int  dso_create(const des_mesh_view *mesh, const des_params *params, dso **out);
 void dso_destroy(dso *o);
 int  dso_set_params(dso *o, const des_params *params);
+/* the counts phase_changes leaves in var.elemmarkers (phasechanges.cxx:232-258) */
+int  dso_set_elemmarkers(dso *o, const int *elemmarkers);
 int  dso_num_threads(void);
 
 /* topology as mesh.cxx builds it (the naive facet scan for small meshes) */

@@ -75,6 +75,7 @@ class PortOracle(_Base):
             L.dso_destroy.argtypes = [C.c_void_p]
             L.dso_destroy.restype = None
             L.dso_set_params.argtypes = [C.c_void_p, P(abi.Params)]
+            L.dso_set_elemmarkers.argtypes = [C.c_void_p, P(C.c_int)]
             L.dso_init_fields.argtypes = [C.c_void_p, P(abi.StateView)]
             L.dso_step.argtypes = [C.c_void_p, P(abi.StateView), C.c_int]
             L.dso_compute_dt.argtypes = [C.c_void_p, P(abi.StateView), P(C.c_double)]
@@ -115,6 +116,12 @@ class PortOracle(_Base):
     def set_params(self, params):
         self.params = params
         self.L.dso_set_params(self.h, C.byref(params))
+
+    def set_elemmarkers(self, elemmarkers):
+        self._em = np.ascontiguousarray(elemmarkers, dtype=np.int32)
+        rc = self.L.dso_set_elemmarkers(self.h, abi.iptr(self._em))
+        if rc:
+            raise RuntimeError(f"dso_set_elemmarkers failed {rc}")
 
     def boundary_normals(self, coord, params):
         rc = self.L.dso_boundary_normals(self.h, abi.dptr(coord), C.byref(params))
@@ -211,6 +218,8 @@ class RefOracle(_Base):
             L.dsr_step.argtypes = [C.c_void_p, C.c_int]
             L.dsr_compute_dt.argtypes = [C.c_void_p]
             L.dsr_compute_dt.restype = C.c_double
+            L.dsr_set_elemmarkers.argtypes = [C.c_void_p, P(C.c_int)]
+            L.dsr_inherit.argtypes = [C.c_void_p, C.c_void_p]
             L.dsr_max_vbc_val.argtypes = [C.c_void_p]
             L.dsr_max_vbc_val.restype = C.c_double
             L.dsr_compensation_pressure.argtypes = [C.c_void_p]
@@ -245,6 +254,15 @@ class RefOracle(_Base):
         v = state.view()
         self.L.dsr_init_fields(self.h, C.byref(v))
         state.sync_scalars(v)
+
+    def set_elemmarkers(self, elemmarkers):
+        em = np.ascontiguousarray(elemmarkers, dtype=np.int32)
+        self.L.dsr_set_elemmarkers(self.h, abi.iptr(em))
+
+    def inherit(self, other):
+        """Boundary normals, edge vectors and compensation pressure of `other`
+        (what remesh keeps across a new mesh)."""
+        self.L.dsr_inherit(self.h, other.h)
 
     def _in(self, state):
         v = state.view()

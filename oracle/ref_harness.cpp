@@ -160,6 +160,17 @@ int dsr_create(const des_mesh_view *m, const des_params *q, dsr **out)
 
 double dsr_max_vbc_val(const dsr *h) { return h->var.max_vbc_val; }
 
+// writes the counts in place, as phase_changes does (phasechanges.cxx:248-254):
+// MatProps holds a reference to var.elemmarkers
+int dsr_set_elemmarkers(dsr *h, const int *em)
+{
+    int_vec2D &k = *h->var.elemmarkers;
+    const int nmat = (int)k[0].size();
+    for (int e = 0; e < h->var.nelem; ++e)
+        for (int m = 0; m < nmat; ++m) k[e][m] = em[(size_t)nmat * e + m];
+    return 0;
+}
+
 int dsr_bcflag(const dsr *h, unsigned *bcflag)
 {
     for (int i = 0; i < h->var.nnode; ++i) bcflag[i] = (*h->var.bcflag)[i];
@@ -201,6 +212,18 @@ int dsr_normals(const dsr *h, double *bnormals30, double *edge300)
     return DES_OK;
 }
 double dsr_compensation_pressure(const dsr *h) { return h->var.compensation_pressure; }
+
+// the Variables members remesh leaves as they were (boundary normals and edge
+// vectors from init, the compensation pressure), for a harness built on the
+// remeshed mesh
+int dsr_inherit(dsr *h, const dsr *from)
+{
+    for (int i = 0; i < nbdrytypes; ++i)
+        for (int d = 0; d < NDIMS; ++d) h->var.bnormals[i][d] = from->var.bnormals[i][d];
+    h->var.edge_vectors = from->var.edge_vectors;
+    h->var.compensation_pressure = from->var.compensation_pressure;
+    return 0;
+}
 
 int dsr_set_state(dsr *h, const des_state_view *s, unsigned mask)
 {

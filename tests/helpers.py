@@ -38,6 +38,72 @@ def layered_config(nx=6, ny=5, nz=6):
     return cfg
 
 
+def phase_config(nx=8, ny=6, nz=6):
+    """Three layers whose materials differ in density, moduli, conductivity,
+    heat capacity and cohesion, so a phase change moves every mixed property;
+    elasto-plastic (no viscosity, whose pow/exp differ from the host's libm by
+    an ulp), so the FP64 form stays bit-identical."""
+    cfg = W.scaled(W.CONFIGS["5"], nx, ny, nz, name=f"phase_{nx}x{ny}x{nz}")
+    cfg.rheology = "ep"
+    cfg.extra = dict(mats=dict(shear_modulus=[30e9, 25e9, 40e9], bulk_modulus=[128e9, 100e9, 150e9],
+                               therm_cond=[3.3, 2.5, 4.0], heat_capacity=[1000.0, 900.0, 1200.0],
+                               cohesion0=[44e6, 30e6, 60e6]))
+    return cfg
+
+
+def phase_change(mesh, state, em):
+    """A deterministic stand-in for a PhaseChange rule (phasechanges.cxx:
+    232-258 moves one marker's count from its old to its new material): in
+    the hotter half of the elements holding material 0, one marker of
+    material 0 becomes material 2; in the deeper half of those holding
+    material 1, one marker of material 1 becomes material 0."""
+    conn = mesh.connectivity
+    T = state.temperature[conn].mean(axis=1)
+    z = state.coord[conn, 2].mean(axis=1)
+    em = em.copy()
+    c0, c1 = em[:, 0] > 0, em[:, 1] > 0
+    hot = c0 & (T > np.median(T[c0])) if c0.any() else c0
+    deep = c1 & (z < np.median(z[c1])) if c1.any() else c1
+    em[hot, 0] -= 1
+    em[hot, 2] += 1
+    em[deep, 1] -= 1
+    em[deep, 0] += 1
+    return em
+
+
+def remesh_standin(mesh, state, elemmarkers, cfg):
+    """A stand-in for the host half of remesh (remeshing.cxx:1970-2013, TetGen
+    and the interpolations): a new box mesh of cfg's resolution; node fields
+    from the nearest old node, element fields and marker counts from the
+    element with the nearest centroid.  Returns the new mesh and its fields."""
+    from scipy.spatial import cKDTree
+    new = W.Mesh(cfg, D.lib())
+    s = abi.State(new.nnode, new.nelem)
+    s.coord[:] = new.coord
+    jn = cKDTree(state.coord).query(new.coord)[1]
+    for f in ("vel", "temperature", "coord0"):
+        getattr(s, f)[:] = getattr(state, f)[jn]
+    old_c = state.coord[mesh.connectivity].mean(axis=1)
+    new_c = new.coord[new.connectivity].mean(axis=1)
+    je = cKDTree(old_c).query(new_c)[1]
+    for f in ("plstrain", "delta_plstrain", "strain", "stress"):
+        getattr(s, f)[:] = getattr(state, f)[je]
+    new.elemmarkers[:] = elemmarkers[je]
+    s.time, s.dt, s.steps = state.time, state.dt, state.steps
+    return new, s
+
+
+def post_remesh(oracle, s, zlength, reset_bottom_coord0):
+    """What remesh does after reallocate_variables (remeshing.cxx:2037-2054),
+    through the oracle's functions."""
+    oracle.call("compute_volume", s)
+    s.volume_old[:] = s.volume
+    oracle.call("compute_mass", s)
+    oracle.call("compute_shape_fn", s)
+    if reset_bottom_coord0:
+        s.coord0[(oracle.bcflag() & 16) != 0, 2] = -zlength
+
+
 class Case:
     def __init__(self, cfg):
         self.cfg = cfg

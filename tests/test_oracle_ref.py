@@ -101,3 +101,63 @@ def test_elem_quality_and_worst_bit_exact():
     assert np.array_equal(q, qr)
     first = int(np.argmin(q)) if q.min() < 1 else 0
     assert w == first and qw == min(1.0, q.min())
+
+
+def test_phase_changes_every_10_steps_bit_exact():
+    """Marker counts changed in place every 10 steps, followed by compute_dt
+    (dynearthsol.cxx:382-393), in the restatement and the reference."""
+    from helpers import phase_config, phase_change
+    c, r = both(phase_config())
+    a = W.new_state(c.mesh, c.T, c.pls)
+    b = W.new_state(c.mesh, c.T, c.pls)
+    c.oracle.init_fields(a)
+    r.init_fields(b)
+    em = c.mesh.elemmarkers.copy()
+    for _ in range(3):
+        c.oracle.step(a, 10)
+        r.step(b, 10)
+        em2 = phase_change(c.mesh, a, em)
+        assert (em2 != em).any()
+        em = em2
+        c.oracle.set_elemmarkers(em)
+        r.set_elemmarkers(em)
+        a.dt = c.oracle.call("compute_dt", a)
+        b.dt = r.call("compute_dt", b)
+        assert a.dt == b.dt
+    c.oracle.step(a, 25)
+    r.step(b, 25)
+    assert not diff_fields(a, b)
+    assert (a.time, a.dt, a.steps) == (b.time, b.dt, b.steps)
+
+
+def test_post_remesh_sequence_and_steps_bit_exact():
+    """After a stand-in remesh, the reference's post-remesh functions
+    (remeshing.cxx:2037-2054) and 20 steps on the new mesh, in the
+    restatement and the reference."""
+    from helpers import phase_config, remesh_standin, post_remesh
+    from oracle.oracle import PortOracle
+    cfg = phase_config()
+    c, r = both(cfg)
+    a = W.new_state(c.mesh, c.T, c.pls)
+    b = W.new_state(c.mesh, c.T, c.pls)
+    c.oracle.init_fields(a)
+    r.init_fields(b)
+    c.oracle.step(a, 20)
+    r.step(b, 20)
+    assert not diff_fields(a, b)
+    new_cfg = W.scaled(cfg, 9, 7, 5)
+    new_cfg.mesh_seed += 17
+    mesh2, s = remesh_standin(c.mesh, a, c.mesh.elemmarkers, new_cfg)
+    p2 = abi.Params.from_buffer_copy(c.params)
+    p2.compensation_pressure = r.compensation_pressure()
+    o2 = PortOracle(mesh2, p2)
+    r2 = RefOracle(mesh2, p2)
+    r2.inherit(r)
+    a2, b2 = s.copy(), s.copy()
+    post_remesh(o2, a2, cfg.zlength, True)
+    post_remesh(r2, b2, cfg.zlength, True)
+    assert not diff_fields(a2, b2, COMPARED + ["coord0"])
+    o2.step(a2, 20)
+    r2.step(b2, 20)
+    assert not diff_fields(a2, b2, COMPARED + ["coord0"])
+    assert (a2.time, a2.dt, a2.steps) == (b2.time, b2.dt, b2.steps)
