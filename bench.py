@@ -518,9 +518,9 @@ def run_ours(args):
         "gpu_launches": dev.kernels_per_step * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
-                     # DRAM bytes per launch: 417 B/element read + written by E-A in the ncu
-                     # capture of profiles/k_fe_a_fp64_box100x100x40.md (traffic grows with the
-                     # element count), scaled to this launch
+                     # DRAM bytes per launch: 417 B/element read + written by E-A in an ncu
+                     # capture on a 100x100x40 box (traffic grows with the element count),
+                     # scaled to this launch
                      "traffic": 417.0 * mesh.nelem if names[top] == "E-A" else None,
                      "peak_kind": hbm_kind,
                      "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,

@@ -109,14 +109,21 @@ des_state_view make_state(Variables &v)
     return s;
 }
 
+// int_vec2D rows of marker counts, one after the other
+std::vector<int> flat_markers(const Param &param, const Variables &var)
+{
+    std::vector<int> markers(static_cast<size_t>(var.nelem) * param.mat.nmat);
+    for (int e = 0; e < var.nelem; ++e)
+        for (int m = 0; m < param.mat.nmat; ++m) markers[static_cast<size_t>(e) * param.mat.nmat + m] = (*var.elemmarkers)[e][m];
+    return markers;
+}
+
 }  // namespace
 
 des_gpu *des_shim_attach(const Param &param, Variables &var)
 {
     des_params q = make_params(param, var);
-    std::vector<int> markers(static_cast<size_t>(var.nelem) * param.mat.nmat);
-    for (int e = 0; e < var.nelem; ++e)
-        for (int m = 0; m < param.mat.nmat; ++m) markers[static_cast<size_t>(e) * param.mat.nmat + m] = (*var.elemmarkers)[e][m];
+    std::vector<int> markers = flat_markers(param, var);
     des_mesh_view mesh = {var.nnode, var.nelem, var.nseg, param.mat.nmat, var.connectivity->data(),
                           var.segment->data(), var.segflag->data(), markers.data()};
     des_gpu *g = nullptr;
@@ -155,4 +162,22 @@ int des_shim_download(des_gpu *g, Variables &var, unsigned mask)
         var.steps = s.steps;
     }
     return rc;
+}
+
+int des_shim_phase_changes(des_gpu *g, const Param &param, Variables &var)
+{
+    std::vector<int> markers = flat_markers(param, var);
+    int rc = des_gpu_set_elemmarkers(g, markers.data());
+    if (rc) return rc;
+    return des_gpu_compute_dt(g, &var.dt);
+}
+
+int des_shim_remeshed(des_gpu *g, const Param &param, Variables &var)
+{
+    std::vector<int> markers = flat_markers(param, var);
+    des_mesh_view mesh = {var.nnode, var.nelem, var.nseg, param.mat.nmat, var.connectivity->data(),
+                          var.segment->data(), var.segflag->data(), markers.data()};
+    des_state_view s = make_state(var);
+    const int opt = param.mesh.remeshing_option;
+    return des_gpu_remesh(g, &mesh, &s, opt == 1 || opt == 2 || opt == 11);
 }

@@ -1,6 +1,6 @@
 // Glue between the reference's Param / Variables (parameters.hpp) and the C
 // ABI of libdes_gb300.so.  Compiled inside the reference's build, against its
-// headers; see INTEGRATION.md.
+// headers.
 #pragma once
 
 #include "des_gpu.h"
@@ -21,3 +21,14 @@ int des_shim_step(des_gpu *g, Variables &var, int nsteps);
 // Copies device fields back into var's arrays before output, checkpoint or
 // remesh (mask: DES_F_* bits, DES_F_ALL for everything).
 int des_shim_download(des_gpu *g, Variables &var, unsigned mask);
+
+// After phase_changes (phasechanges.cxx:232-258) at steps % 10 == 0: the
+// device takes var.elemmarkers and recomputes dt as compute_dt does right
+// after it (dynearthsol.cxx:382-393); var.dt is updated.
+int des_shim_phase_changes(des_gpu *g, const Param &param, Variables &var);
+
+// After the reference's remesh (remeshing.cxx:1963-2067) has run on var's
+// host arrays (download them first): the device takes the new mesh, the
+// interpolated fields and the remapped markers, and repeats remesh's
+// compute_volume / compute_mass / compute_shape_fn / coord0 reset.
+int des_shim_remeshed(des_gpu *g, const Param &param, Variables &var);
