@@ -714,6 +714,13 @@ __device__ __forceinline__ double min_height(const double X[4][3], double vol)
     return 3 * vol / maxa;
 }
 
+// !(x > 0) from the bits (integer pipes): zero, negative or NaN
+__device__ __forceinline__ bool not_positive(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b <= 0 || b > 0x7ff0000000000000ll;
+}
+
 // true for NaN or +-Inf, from the exponent bits (integer pipes)
 __device__ __forceinline__ bool not_finite(double x)
 {

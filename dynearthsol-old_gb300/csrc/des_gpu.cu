@@ -20,6 +20,7 @@ namespace {
 const int kElemBlock = 128;
 const int kNodeBlock = 256;
 const int kStepKernels = 6;
+const int kEaChunks = 8;   // E-A launches of the host-buffer step (downloads overlap them)
 
 inline int blocks(long long n, int b) { return (int)((n + b - 1) / b); }
 
@@ -57,6 +58,9 @@ struct des_gpu {
     unsigned snap_mask = 0;
     Clock *snap_clk = nullptr;
     cudaStream_t copy_stream = nullptr;
+    double *dl = nullptr;                 // host-layout rows of an overlapped download
+    long long dl_elems = 0;
+    cudaEvent_t head_done = nullptr;      // a step's passes before E-A are done
     cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
     int avg_interval = 0;                 // Output::average_fields every step when > 0
     double *avg_c0 = nullptr, *avg_strain0 = nullptr, *avg_stress = nullptr, *avg_dpls = nullptr,
@@ -328,6 +332,7 @@ int build_consts(des_gpu *g)
                 nn += x.count[m];
             }
             y.rho_ref = rr / nn;
+            y.rho_g4 = y.rho_ref * p.gravity / 4;
             y.rho_alpha = (float)(ra / nn);
             y.single = x.single;
             y.n = x.n;
@@ -408,17 +413,18 @@ int upload_field(des_gpu *g, const double *host, double *dst, int ncomp, long lo
     }
     return DES_OK;
 }
-int download_field(des_gpu *g, double *host, const double *src, int ncomp, long long rows)
+// device SoA -> host rows through the staging buffer stg, on stream st
+int download_field(des_gpu *g, double *host, const double *src, int ncomp, long long rows,
+                   cudaStream_t st, double *stg)
 {
     if (!host) return DES_ERR_ARG;
     long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
     for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
         long long nr = std::min(chunk_rows, rows - r0);
-        k_soa_to_aos<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(src, g->staging, ncomp, nr, r0,
-                                                                       rows);
+        k_soa_to_aos<<<blocks(nr * ncomp, 256), 256, 0, st>>>(src, stg, ncomp, nr, r0, rows);
         DES_LAUNCH();
-        DES_CUDA(cudaMemcpyAsync(host + r0 * ncomp, g->staging, sizeof(double) * nr * ncomp,
-                                 cudaMemcpyDeviceToHost, g->stream));
+        DES_CUDA(cudaMemcpyAsync(host + r0 * ncomp, stg, sizeof(double) * nr * ncomp,
+                                 cudaMemcpyDeviceToHost, st));
     }
     return DES_OK;
 }
@@ -442,21 +448,6 @@ int upload_field(des_gpu *g, const double *host, float *dst, int ncomp, long lon
     }
     return DES_OK;
 }
-int download_field(des_gpu *g, double *host, const float *src, int ncomp, long long rows)
-{
-    if (!host) return DES_ERR_ARG;
-    long long chunk_rows = std::max(1LL, g->staging_elems / ncomp);
-    for (long long r0 = 0; r0 < rows; r0 += chunk_rows) {
-        long long nr = std::min(chunk_rows, rows - r0);
-        k_soa_to_aos_f<<<blocks(nr * ncomp, 256), 256, 0, g->stream>>>(src, g->staging, ncomp, nr,
-                                                                         r0, rows);
-        DES_LAUNCH();
-        DES_CUDA(cudaMemcpyAsync(host + r0 * ncomp, g->staging, sizeof(double) * nr * ncomp,
-                                 cudaMemcpyDeviceToHost, g->stream));
-    }
-    return DES_OK;
-}
-
 int read_clock(des_gpu *g, Clock &c)
 {
     DES_CUDA(cudaMemcpyAsync(&c, g->dclk, sizeof(Clock), cudaMemcpyDeviceToHost, g->stream));
@@ -503,8 +494,8 @@ int prime(des_gpu *g)
     return DES_OK;
 }
 
-// the six passes of one step, in order, on g's stream (captured or not)
-void launch_step(des_gpu *g, cudaEvent_t *ev)
+// passes N-A .. N-C of one step
+void launch_head(des_gpu *g, cudaEvent_t *ev)
 {
     const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
     cudaStream_t st = g->stream;
@@ -525,8 +516,6 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
         kf_fe_c<<<eb, kElemBlock, 0, st>>>(f);
         if (ev) cudaEventRecord(ev[4], st);
         kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f);
-        if (ev) cudaEventRecord(ev[5], st);
-        kf_fe_a<<<eb, kElemBlock, 0, st>>>(f);
     } else {
         const Dev &d = g->d;
         k_fn_a<<<nb, kNodeBlock, 0, st>>>(d);
@@ -541,10 +530,23 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
         k_fe_c<<<eb, kElemBlock, 0, st>>>(d);
         if (ev) cudaEventRecord(ev[4], st);
         k_fn_c<<<nb, kNodeBlock, 0, st>>>(d);
-        if (ev) cudaEventRecord(ev[5], st);
-        k_fe_a<<<eb, kElemBlock, 0, st>>>(d);
     }
-    if (ev) cudaEventRecord(ev[6], st);
+}
+
+// E-A over the element blocks [b0, b1) of its nblocks
+void launch_ea(des_gpu *g, int b0, int b1)
+{
+    const int nb = blocks(g->nelem, kElemBlock);
+    if (g->prec == DES_PREC_FP32)
+        kf_fe_a<<<b1 - b0, kElemBlock, 0, g->stream>>>(g->f, b0 * kElemBlock, nb);
+    else
+        k_fe_a<<<b1 - b0, kElemBlock, 0, g->stream>>>(g->d, b0 * kElemBlock, nb);
+}
+
+// the averaging of the output fields after a step (Output::average_fields)
+void launch_average(des_gpu *g)
+{
+    cudaStream_t st = g->stream;
     if (g->avg_interval > 0) {
         AvgArgs a;
         a.nnode = g->nnode;
@@ -570,10 +572,51 @@ void launch_step(des_gpu *g, cudaEvent_t *ev)
     }
 }
 
+// pass E-A (and the averaging of the output fields) of one step
+void launch_tail(des_gpu *g, cudaEvent_t *ev)
+{
+    if (ev) cudaEventRecord(ev[5], g->stream);
+    launch_ea(g, 0, blocks(g->nelem, kElemBlock));
+    if (ev) cudaEventRecord(ev[6], g->stream);
+    launch_average(g);
+}
+
+// the six passes of one step, in order, on g's stream (captured or not)
+void launch_step(des_gpu *g, cudaEvent_t *ev)
+{
+    launch_head(g, ev);
+    launch_tail(g, ev);
+}
+
 int finish(des_gpu *g)
 {
     DES_CUDA(cudaGetLastError());
     DES_CUDA(cudaStreamSynchronize(g->stream));
+    return DES_OK;
+}
+
+// the second stream (output copies, downloads overlapping E-A) and its events
+int ensure_copy_stream(des_gpu *g)
+{
+    if (!g->copy_stream) DES_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+    if (!g->head_done) DES_CUDA(cudaEventCreateWithFlags(&g->head_done, cudaEventDisableTiming));
+    return DES_OK;
+}
+
+// the overlapped download's buffer, grown to n doubles when smaller
+int ensure_download_buffer(des_gpu *g, long long n)
+{
+    if (n <= g->dl_elems) return DES_OK;
+    if (g->dl) {
+        g->allocs.erase(std::find(g->allocs.begin(), g->allocs.end(), static_cast<void *>(g->dl)));
+        g->bytes -= (long long)sizeof(double) * (g->dl_elems ? g->dl_elems : 1);
+        DES_CUDA(cudaFree(g->dl));
+        g->dl = nullptr;
+        g->dl_elems = 0;
+    }
+    int rc = dev_alloc(g, &g->dl, (size_t)n);
+    if (rc) return rc;
+    g->dl_elems = n;
     return DES_OK;
 }
 
@@ -760,6 +803,7 @@ int des_gpu_destroy(des_gpu *g)
         cudaStreamDestroy(g->copy_stream);
     }
     if (g->snap_ready) cudaEventDestroy(g->snap_ready);
+    if (g->head_done) cudaEventDestroy(g->head_done);
     if (g->snap_done) cudaEventDestroy(g->snap_done);
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->graph) cudaGraphExecDestroy(g->graph);
@@ -895,72 +939,147 @@ int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
     return finish(g);
 }
 
+// One field of a download: its host rows and its device source (FP64 or
+// FP32 structure of arrays, or the FP32 form's split stress s0 + s').
+struct DownPart {
+    double *host;
+    const double *src64;
+    const float *src32;
+    bool stress_join;
+    int ncomp;
+    long long rows;
+    bool elem;          // one row per element (else per node)
+};
+
+// the mask fields in download order; DES_ERR_ARG for a missing host array
+static int down_parts(des_gpu *g, des_state_view *h, unsigned mask, std::vector<DownPart> &out)
+{
+    const long long N = g->nnode, E = g->nelem;
+    const Dev &d = g->d;
+    const DevF &f = g->f;
+    const bool f32 = g->prec == DES_PREC_FP32;
+    out.clear();
+    bool ok = true;
+    // x: a field kept in the form's precision (FP32 in the mixed form)
+    auto add = [&](unsigned flag, double *host, const double *s64, const float *s32, bool x, int nc, bool elem) {
+        if (!ok || !(mask & flag)) return;
+        if (!host) {
+            ok = false;
+            return;
+        }
+        const bool use32 = x && f32;
+        out.push_back({host, use32 ? nullptr : s64, use32 ? s32 : nullptr, false, nc, elem ? E : N, elem});
+    };
+    add(DES_F_COORD, h->coord, d.x, nullptr, false, 3, false);
+    add(DES_F_COORD0, h->coord0, d.x0, nullptr, false, 3, false);
+    add(DES_F_VEL, h->vel, d.vx, f.vx, true, 3, false);
+    add(DES_F_FORCE, h->force, d.fx, f.fx, true, 3, false);
+    add(DES_F_TEMPERATURE, h->temperature, d.T, nullptr, false, 1, false);
+    add(DES_F_MASS, h->mass, d.mass, f.mass, true, 1, false);
+    add(DES_F_MASS, h->tmass, d.tmass, f.tmass, true, 1, false);
+    add(DES_F_MASS, h->volume_n, d.vol_n, f.vol_n, true, 1, false);
+    add(DES_F_NTMP, h->ntmp, d.ntmp, f.ntmp, true, 1, false);
+    add(DES_F_VOLUME, h->volume, d.vol, nullptr, false, 1, true);
+    add(DES_F_VOLUME, h->volume_old, d.vol_old, nullptr, false, 1, true);
+    if (ok && (mask & DES_F_STRESS)) {
+        if (!h->stress) return DES_ERR_ARG;
+        out.push_back({h->stress, f32 ? nullptr : d.stress, nullptr, f32, 6, E, true});
+    }
+    add(DES_F_STRAIN, h->strain, d.strain, f.strain, true, 6, true);
+    add(DES_F_STRAIN_RATE, h->strain_rate, d.srate, f.srate, true, 6, true);
+    add(DES_F_PLSTRAIN, h->plstrain, d.pls, nullptr, false, 1, true);
+    add(DES_F_PLSTRAIN, h->delta_plstrain, d.dpls, f.dpls, true, 1, true);
+    add(DES_F_DPRESSURE, h->dpressure, d.dp, f.dp, true, 1, true);
+    add(DES_F_EDVOLDT, h->edvoldt, d.edvoldt, f.edvoldt, true, 1, true);
+    add(DES_F_SHAPE, h->shpdx, d.shp, f.shp, true, 4, true);
+    add(DES_F_SHAPE, h->shpdy, d.shp + 4 * E, f.shp + 4 * E, true, 4, true);
+    add(DES_F_SHAPE, h->shpdz, d.shp + 8 * E, f.shp + 8 * E, true, 4, true);
+    add(DES_F_TMP_RESULT, h->tmp_result, d.tmp, f.tmp, true, 12, true);
+    add(DES_F_TMP_RESULT, h->tmp_result_sg, d.tmp_sg, f.tmp_sg, true, 1, true);
+    return ok ? DES_OK : DES_ERR_ARG;
+}
+
+// rows [r0, r0 + nr) of one part as host-layout rows at dst, on stream st
+static int convert_part(des_gpu *g, const DownPart &q, long long r0, long long nr, double *dst, cudaStream_t st)
+{
+    if (q.stress_join)
+        k_stress_join<<<blocks(nr, 256), 256, 0, st>>>(g->f.s0, g->f.stress, dst, nr, r0, q.rows);
+    else if (q.src64)
+        k_soa_to_aos<<<blocks(nr * q.ncomp, 256), 256, 0, st>>>(q.src64, dst, q.ncomp, nr, r0, q.rows);
+    else
+        k_soa_to_aos_f<<<blocks(nr * q.ncomp, 256), 256, 0, st>>>(q.src32, dst, q.ncomp, nr, r0, q.rows);
+    DES_LAUNCH();
+    return DES_OK;
+}
+
+// The mask fields into the host rows through the staging buffer, on g's
+// stream (current nodal masses and the clock are the caller's part).
+static int download_fields(des_gpu *g, des_state_view *h, unsigned mask)
+{
+    std::vector<DownPart> parts;
+    int rc = down_parts(g, h, mask, parts);
+    if (rc) return rc;
+    for (const DownPart &q : parts) {
+        const long long chunk = std::max(1LL, g->staging_elems / q.ncomp);
+        for (long long r0 = 0; r0 < q.rows; r0 += chunk) {
+            const long long nr = std::min(chunk, q.rows - r0);
+            if ((rc = convert_part(g, q, r0, nr, g->staging, g->stream))) return rc;
+            DES_CUDA(cudaMemcpyAsync(q.host + r0 * q.ncomp, g->staging, sizeof(double) * nr * q.ncomp,
+                                     cudaMemcpyDeviceToHost, g->stream));
+        }
+    }
+    return DES_OK;
+}
+
+// Overlapped form: each part is converted whole on g's stream into the
+// download buffer at *offset and copied to the host on the copy stream as
+// soon as its conversion is done, so conversions, copies and later kernels
+// of g's stream run side by side.  The caller synchronises the copy stream.
+// rows [r0, r0 + nr) of part q: converted on g's stream into its place in
+// the download buffer (the part starts at base), then copied on the copy stream
+static int download_rows_async(des_gpu *g, const DownPart &q, long long base, long long r0, long long nr)
+{
+    double *dst = g->dl + base + r0 * q.ncomp;
+    int rc = convert_part(g, q, r0, nr, dst, g->stream);
+    if (rc) return rc;
+    DES_CUDA(cudaEventRecord(g->head_done, g->stream));
+    DES_CUDA(cudaStreamWaitEvent(g->copy_stream, g->head_done, 0));
+    DES_CUDA(cudaMemcpyAsync(q.host + r0 * q.ncomp, dst, sizeof(double) * q.ncomp * nr, cudaMemcpyDeviceToHost,
+                             g->copy_stream));
+    return DES_OK;
+}
+
+static int download_async(des_gpu *g, const std::vector<DownPart> &parts, long long *offset)
+{
+    for (const DownPart &q : parts) {
+        int rc = download_rows_async(g, q, *offset, 0, q.rows);
+        if (rc) return rc;
+        *offset += q.ncomp * q.rows;
+    }
+    return DES_OK;
+}
+
+// nodal masses from the last E-A's contributions, before they are read
+static int flush_masses(des_gpu *g, const Clock &c)
+{
+    if (c.mass_valid) return DES_OK;
+    if (g->prec == DES_PREC_FP32)
+        kf_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->f);
+    else
+        k_mass_flush<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
+    DES_LAUNCH();
+    return DES_OK;
+}
+
 int des_gpu_download(des_gpu *g, des_state_view *h, unsigned mask)
 {
     if (!g || !h || h->nnode != g->nnode || h->nelem != g->nelem) return DES_ERR_ARG;
     if (mask & ~(unsigned)DES_F_ALL) return DES_ERR_ARG;
-    const long long N = g->nnode, E = g->nelem;
-    Dev &d = g->d;
     Clock c;
     int rc = read_clock(g, c);
     if (rc) return rc;
-    const bool f32 = g->prec == DES_PREC_FP32;
-    DevF &f = g->f;
-    if ((mask & DES_F_MASS) && !c.mass_valid) {
-        if (f32)
-            kf_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(f);
-        else
-            k_mass_flush<<<blocks(N, kNodeBlock), kNodeBlock, 0, g->stream>>>(d);
-        DES_LAUNCH();
-    }
-#define DOWN(flag, ptr, src, nc, rows) \
-    if ((mask & (flag)) && (rc = download_field(g, h->ptr, src, nc, rows))) return rc;
-#define DOWNX(flag, ptr, fld, off, nc, rows)                                                  \
-    if (mask & (flag)) {                                                                     \
-        rc = f32 ? download_field(g, h->ptr, f.fld + (off), nc, rows)                        \
-                 : download_field(g, h->ptr, d.fld + (off), nc, rows);                       \
-        if (rc) return rc;                                                                   \
-    }
-    DOWN(DES_F_COORD, coord, d.x, 3, N)
-    DOWN(DES_F_COORD0, coord0, d.x0, 3, N)
-    DOWNX(DES_F_VEL, vel, vx, 0, 3, N)
-    DOWNX(DES_F_FORCE, force, fx, 0, 3, N)
-    DOWN(DES_F_TEMPERATURE, temperature, d.T, 1, N)
-    DOWNX(DES_F_MASS, mass, mass, 0, 1, N)
-    DOWNX(DES_F_MASS, tmass, tmass, 0, 1, N)
-    DOWNX(DES_F_MASS, volume_n, vol_n, 0, 1, N)
-    DOWNX(DES_F_NTMP, ntmp, ntmp, 0, 1, N)
-    DOWN(DES_F_VOLUME, volume, d.vol, 1, E)
-    DOWN(DES_F_VOLUME, volume_old, d.vol_old, 1, E)
-    if (mask & DES_F_STRESS) {
-        if (f32) {
-            if (!h->stress) return DES_ERR_ARG;
-            long long chunk = std::max(1LL, g->staging_elems / 6);
-            for (long long r0 = 0; r0 < E; r0 += chunk) {
-                long long nr = std::min(chunk, E - r0);
-                k_stress_join<<<blocks(nr, 256), 256, 0, g->stream>>>(f.s0, f.stress, g->staging, nr,
-                                                                       r0, E);
-                DES_LAUNCH();
-                DES_CUDA(cudaMemcpyAsync(h->stress + 6 * r0, g->staging, sizeof(double) * 6 * nr,
-                                         cudaMemcpyDeviceToHost, g->stream));
-            }
-        } else if ((rc = download_field(g, h->stress, d.stress, 6, E))) {
-            return rc;
-        }
-    }
-    DOWNX(DES_F_STRAIN, strain, strain, 0, 6, E)
-    DOWNX(DES_F_STRAIN_RATE, strain_rate, srate, 0, 6, E)
-    DOWN(DES_F_PLSTRAIN, plstrain, d.pls, 1, E)
-    DOWNX(DES_F_PLSTRAIN, delta_plstrain, dpls, 0, 1, E)
-    DOWNX(DES_F_DPRESSURE, dpressure, dp, 0, 1, E)
-    DOWNX(DES_F_EDVOLDT, edvoldt, edvoldt, 0, 1, E)
-    DOWNX(DES_F_SHAPE, shpdx, shp, 0, 4, E)
-    DOWNX(DES_F_SHAPE, shpdy, shp, 4 * E, 4, E)
-    DOWNX(DES_F_SHAPE, shpdz, shp, 8 * E, 4, E)
-    DOWNX(DES_F_TMP_RESULT, tmp_result, tmp, 0, 12, E)
-    DOWNX(DES_F_TMP_RESULT, tmp_result_sg, tmp_sg, 0, 1, E)
-#undef DOWN
-#undef DOWNX
+    if ((mask & DES_F_MASS) && (rc = flush_masses(g, c))) return rc;
+    if ((rc = download_fields(g, h, mask))) return rc;
     if (mask & DES_F_SCALARS) {
         h->time = c.time;
         h->dt = c.dt;
@@ -1113,7 +1232,7 @@ int des_gpu_output_snapshot(des_gpu *g, unsigned mask)
         int rc;
         if ((rc = dev_alloc(g, &g->snap, (size_t)n)) || (rc = dev_alloc(g, &g->snap_clk, 1))) return rc;
         g->snap_bytes = n * (long long)sizeof(double);
-        DES_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
+        if ((rc = ensure_copy_stream(g))) return rc;
         DES_CUDA(cudaEventCreateWithFlags(&g->snap_ready, cudaEventDisableTiming));
         DES_CUDA(cudaEventCreateWithFlags(&g->snap_done, cudaEventDisableTiming));
         DES_CUDA(cudaEventRecord(g->snap_done, g->copy_stream));
@@ -1222,10 +1341,11 @@ int des_gpu_download_averages(des_gpu *g, double *coord0, double *strain0, doubl
     if (!g) return DES_ERR_ARG;
     if (!g->avg_c0) return DES_ERR_UNSUPPORTED;
     int rc;
-    if (coord0 && (rc = download_field(g, coord0, g->avg_c0, 3, g->nnode))) return rc;
-    if (strain0 && (rc = download_field(g, strain0, g->avg_strain0, 6, g->nelem))) return rc;
-    if (stress_sum && (rc = download_field(g, stress_sum, g->avg_stress, 6, g->nelem))) return rc;
-    if (dpls_sum && (rc = download_field(g, dpls_sum, g->avg_dpls, 1, g->nelem))) return rc;
+    if (coord0 && (rc = download_field(g, coord0, g->avg_c0, 3, g->nnode, g->stream, g->staging))) return rc;
+    if (strain0 && (rc = download_field(g, strain0, g->avg_strain0, 6, g->nelem, g->stream, g->staging))) return rc;
+    if (stress_sum && (rc = download_field(g, stress_sum, g->avg_stress, 6, g->nelem, g->stream,
+                                                 g->staging))) return rc;
+    if (dpls_sum && (rc = download_field(g, dpls_sum, g->avg_dpls, 1, g->nelem, g->stream, g->staging))) return rc;
     if (time0) DES_CUDA(cudaMemcpyAsync(time0, g->avg_time0, sizeof(double), cudaMemcpyDeviceToHost, g->stream));
     return finish(g);
 }
@@ -1401,6 +1521,11 @@ void des_abi_sizes(long long out[5])
 // des_gpu_step_host downloads but does not upload them
 constexpr unsigned kStepOutputs =
     DES_F_FORCE | DES_F_NTMP | DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT | DES_F_TMP_RESULT;
+// fields a step has finished before its last pass: E-A writes none of them
+// (coordinates, velocity and temperature it only reads)
+constexpr unsigned kBeforeLastPass = DES_F_COORD | DES_F_COORD0 | DES_F_VEL | DES_F_FORCE |
+                                     DES_F_TEMPERATURE | DES_F_NTMP | DES_F_PLSTRAIN |
+                                     DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT;
 
 // volume, shape derivatives and nodal masses from the device's coordinates
 // and temperature, the values update_mesh (dynearthsol.cxx:237-261) leaves
@@ -1429,7 +1554,7 @@ static int derive_geometry(des_gpu *g)
 int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
                       des_step_report *report)
 {
-    if (!g || !host) return DES_ERR_ARG;
+    if (!g || !host || nsteps < 0) return DES_ERR_ARG;
     unsigned up = mask & ~kStepOutputs;
     // with coordinates and temperature in hand, volume, shape derivatives and
     // masses are recomputed on the device rather than copied (1.0 GB fewer
@@ -1444,9 +1569,64 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
         if ((rc = upload_field(g, host->volume_old, g->d.vol_old, 1, g->nelem))) return rc;
         if ((rc = derive_geometry(g))) return rc;
     }
-    rc = des_gpu_step(g, nsteps, report);
+    if (nsteps == 0) return des_gpu_download(g, host, mask);
+    // every step but the last as the graph; the last as its passes, so that
+    // the fields finished before E-A download on the copy stream while E-A
+    // runs (the host link is the bound of this entry point)
+    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (nsteps > 1 && (rc = des_gpu_step(g, nsteps - 1, nullptr))) return rc;
+    if ((rc = prime(g))) return rc;
+    std::vector<DownPart> early, late;
+    if ((rc = down_parts(g, host, mask & kBeforeLastPass, early)) ||
+        (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)))
+        return rc;
+    long long need = 0;
+    for (const DownPart &q : early) need += q.ncomp * q.rows;
+    for (const DownPart &q : late) need += q.ncomp * q.rows;
+    if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, need))) return rc;
+    std::vector<DownPart> late_elem, late_node;
+    for (const DownPart &q : late) (q.elem ? late_elem : late_node).push_back(q);
+    launch_head(g, nullptr);
+    DES_LAUNCH();
+    long long off = 0;
+    rc = download_async(g, early, &off);
+    // E-A in element chunks; each chunk's rows of the element fields go to
+    // the host while the next chunk computes
+    const int nb = blocks(g->nelem, kElemBlock), nchunk = std::min(kEaChunks, nb);
+    std::vector<long long> base(late_elem.size());
+    for (size_t i = 0; i < late_elem.size(); ++i) {
+        base[i] = off;
+        off += late_elem[i].ncomp * late_elem[i].rows;
+    }
+    for (int k = 0; k < nchunk && !rc; ++k) {
+        const int b0 = (int)((long long)nb * k / nchunk), b1 = (int)((long long)nb * (k + 1) / nchunk);
+        launch_ea(g, b0, b1);
+        rc = cuda_rc(cudaGetLastError());
+        const long long r0 = (long long)b0 * kElemBlock;
+        const long long r1 = std::min<long long>((long long)b1 * kElemBlock, g->nelem);
+        for (size_t i = 0; i < late_elem.size() && !rc; ++i)
+            rc = download_rows_async(g, late_elem[i], base[i], r0, r1 - r0);
+    }
+    if (!rc) {
+        launch_average(g);
+        rc = cuda_rc(cudaGetLastError());
+    }
+    Clock c = {};
+    if (!rc) rc = read_clock(g, c);
+    if (!rc && report && (rc = des_gpu_report(g, report)) == DES_OK &&
+        (report->status & (DES_STATUS_DT_NONPOSITIVE | DES_STATUS_NONFINITE)))
+        rc = DES_ERR_DT;
+    if (!rc && (mask & DES_F_MASS)) rc = flush_masses(g, c);
+    if (!rc) rc = download_async(g, late_node, &off);
+    const cudaError_t ce = cudaStreamSynchronize(g->copy_stream);
     if (rc) return rc;
-    return des_gpu_download(g, host, mask);
+    if (ce != cudaSuccess) return DES_ERR_CUDA;
+    if (mask & DES_F_SCALARS) {
+        host->time = c.time;
+        host->dt = c.dt;
+        host->steps = c.steps;
+    }
+    return finish(g);
 }
 
 // remesh (remeshing.cxx:1963-2067) after the host's new mesh, interpolation

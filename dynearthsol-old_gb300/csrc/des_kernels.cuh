@@ -373,7 +373,11 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, R v[3])
 
 // block-level minimum of two values + the last block turns the global minima
 // into dt (geometry.cxx:311-325).  No thread waits on another block.
-__device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff, bool active)
+// nblocks: the blocks of every launch that contributes (E-A may run as
+// several launches over consecutive element ranges); the last to finish
+// forms dt
+__device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff, bool active,
+                                       unsigned nblocks)
 {
     __shared__ unsigned long long s_min[32], s_dif[32];
     __shared__ bool s_last;
@@ -401,7 +405,7 @@ __device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff,
         if (mb != ~0ULL) atomicMin(&d.clk->dtdiff, mb);
         __threadfence();
         unsigned done = atomicAdd(&d.clk->blocks_done, 1u);
-        s_last = (done == gridDim.x - 1);
+        s_last = (done == nblocks - 1);
     }
     __syncthreads();
     if (s_last && threadIdx.x == 0) {
@@ -761,7 +765,7 @@ __global__ void k_dt(Dev d)
         minh = min_height(X, d.vol[e]);
         dtd = 0.5 * minh * minh / d.K->therm_diff_max;
     }
-    dt_reduce_and_finalize(d, minh, dtd, live);
+    dt_reduce_and_finalize(d, minh, dtd, live, gridDim.x);
 }
 
 // ic.cxx:100-131 (ref_pressure_option 0)
@@ -991,10 +995,12 @@ __global__ void k_fn_c(Dev d)
     if (not_finite(x) || not_finite(y) || not_finite(z)) atomicOr(&d.clk->status, 0x2u);
 }
 
-// E-A: update_mesh element half, rotate_stress, next-step contributions, dt
-__global__ void k_fe_a(Dev d)
+// E-A: update_mesh element half, rotate_stress, next-step contributions, dt;
+// this launch covers the elements from e0 (a multiple of the block size), the
+// pass nblocks blocks in all
+__global__ void k_fe_a(Dev d, int e0, unsigned nblocks)
 {
-    int e = gtid();
+    int e = e0 + gtid();
     const Consts &K = *d.K;
     const bool dt_step = (K.fixed_dt == 0) && (d.clk->steps % 10 == 0);
     if (e == 0) d.clk->mass_valid = 0;
@@ -1008,7 +1014,7 @@ __global__ void k_fe_a(Dev d)
         double vol = tet_volume(X[0], X[1], X[2], X[3]);
         d.vol_old[e] = d.vol[e];
         d.vol[e] = vol;
-        if (!(vol > 0)) atomicOr(&d.clk->status, 0x4u);
+        if (not_positive(vol)) atomicOr(&d.clk->status, 0x4u);
         double dx[4], dy[4], dz[4];
         shape_fn(X, vol, dx, dy, dz);
         store_shp(d, e, dx, dy, dz);
@@ -1040,7 +1046,7 @@ __global__ void k_fe_a(Dev d)
             dtd = 0.5 * minh * minh / K.therm_diff_max;
         }
     }
-    if (dt_step) dt_reduce_and_finalize(d, minh, dtd, live);
+    if (dt_step) dt_reduce_and_finalize(d, minh, dtd, live, nblocks);
 }
 
 // nodal masses from the fused-pass contributions (used before a download)

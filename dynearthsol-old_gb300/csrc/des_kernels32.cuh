@@ -32,6 +32,7 @@ struct MixF {
     float bulkm, shearm, cp, k, rho_qs;
     float rho_alpha;        // sum_m k_m rho0_m alpha_m / n: thermal part of the density
     double rho_ref;         // sum_m k_m rho0_m / n: density at 273 K
+    double rho_g4;          // rho_ref g / 4: an element's buoyancy per node and unit volume
     int single;
     int count[kMaxMat];
     int n;
@@ -370,7 +371,7 @@ __device__ __forceinline__ void f_reference_force(const DevF &d, int e, const do
 {
     const size_t E = d.nelem;
     const double s6 = d.s0[e] * (1.0 / 6.0);
-    const double buoy = d.F->gravity != 0.f ? d.F->mix[d.mix[e]].rho_ref * d.K->gravity / 4 * vol : 0.0;
+    const double buoy = d.F->gravity != 0.f ? d.F->mix[d.mix[e]].rho_g4 * vol : 0.0;
     for (int i = 0; i < 4; ++i) {
         d.f0[(i)*E + e] = s6 * cf[i][0];
         d.f0[(i + 4) * E + e] = s6 * cf[i][1];
@@ -617,16 +618,23 @@ __global__ void kf_fn_c(DevF d)
 }
 
 // FP64 volume and shape derivatives of one element, rounded to FP32 for use;
-// also forms f0 from the FP64 derivatives
-__device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, double X[4][3], float dx[4],
-                                             float dy[4], float dz[4])
+// also forms f0 from the FP64 derivatives.  With c2max, the largest squared
+// cofactor norm: |c_i| is twice the area of the face opposite node i.
+__device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, float dx[4], float dy[4],
+                                             float dz[4], double *c2max)
 {
     const size_t E = d.nelem;
+    double X[4][3];
     f_load_xyz4(d, c, X);
     double cf[4][3];
     const double det = f_cofactors(X, cf);
     const double vol = det * (1.0 / 6.0);
     f_reference_force(d, e, cf, vol);
+    if (c2max) {
+        double m = 0;
+        for (int i = 0; i < 4; ++i) m = fmax(m, fma(cf[i][0], cf[i][0], fma(cf[i][1], cf[i][1], cf[i][2] * cf[i][2])));
+        *c2max = m;
+    }
     // the gradients themselves are FP32: c_i / (6 V)
     const float iv = 1.f / (float)det;
     for (int i = 0; i < 4; ++i) {
@@ -640,10 +648,11 @@ __device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, doubl
     return vol;
 }
 
-// E-A
-__global__ void kf_fe_a(DevF d)
+// E-A, over the elements from e0 (a multiple of the block size); the pass
+// has nblocks blocks in all
+__global__ void kf_fe_a(DevF d, int e0, unsigned nblocks)
 {
-    int e = gtid();
+    int e = e0 + gtid();
     const Consts &K = *d.K;
     const ConstsF &F = *d.F;
     const bool dt_step = (K.fixed_dt == 0) && (d.clk->steps % 10 == 0);
@@ -653,12 +662,12 @@ __global__ void kf_fe_a(DevF d)
     if (live) {
         const size_t E = d.nelem;
         int4 c = d.conn[e];
-        double X[4][3];
         float dx[4], dy[4], dz[4];
-        double vol = f_geometry(d, e, c, X, dx, dy, dz);
+        double c2max = 0;
+        double vol = f_geometry(d, e, c, dx, dy, dz, dt_step ? &c2max : nullptr);
         d.vol_old[e] = d.vol[e];
         d.vol[e] = vol;
-        if (!(vol > 0)) atomicOr(&d.clk->status, 0x4u);
+        if (not_positive(vol)) atomicOr(&d.clk->status, 0x4u);
         float volf = (float)vol;
         d.c_vol[e] = volf;
         const MixF &xf = F.mix[d.mix[e]];
@@ -682,7 +691,9 @@ __global__ void kf_fe_a(DevF d)
         }
         f_next_contrib(d, e, c, V, dx, dy, dz, volf);
         if (dt_step) {
-            minh = min_height(X, vol);
+            // the reference's 3 V / (largest face area) (geometry.cxx:280-293)
+            // from the cofactors: 6 V / max |c_i|
+            minh = 6 * vol / sqrt(c2max);
             dtd = 0.5 * minh * minh / K.therm_diff_max;
         }
     }
@@ -693,7 +704,7 @@ __global__ void kf_fe_a(DevF d)
         dd.mix = d.mix;
         dd.K = d.K;
         dd.clk = d.clk;
-        dt_reduce_and_finalize(dd, minh, dtd, live);
+        dt_reduce_and_finalize(dd, minh, dtd, live, nblocks);
     }
 }
 
@@ -723,9 +734,8 @@ __global__ void kf_init_geometry(DevF d)
     int e = gtid();
     if (e >= d.nelem) return;
     int4 c = d.conn[e];
-    double X[4][3];
     float dx[4], dy[4], dz[4];
-    double vol = f_geometry(d, e, c, X, dx, dy, dz);
+    double vol = f_geometry(d, e, c, dx, dy, dz, nullptr);
     d.vol[e] = vol;
     d.vol_old[e] = vol;
     float volf = (float)vol;
@@ -745,9 +755,8 @@ __global__ void kf_derive_geometry(DevF d)
     int e = gtid();
     if (e >= d.nelem) return;
     int4 c = d.conn[e];
-    double X[4][3];
     float dx[4], dy[4], dz[4];
-    double vol = f_geometry(d, e, c, X, dx, dy, dz);
+    double vol = f_geometry(d, e, c, dx, dy, dz, nullptr);
     d.vol[e] = vol;
     float volf = (float)vol;
     d.c_vol[e] = volf;

@@ -276,7 +276,11 @@ int  des_gpu_step(des_gpu *g, int nsteps, des_step_report *report);
  * recomputed on the device from the uploaded coordinates and temperature
  * (update_mesh's own arithmetic, so the values equal what the previous step
  * left) and only volume_old is copied.  Page-locked host arrays
- * (des_host_register) are read in place by the upload. */
+ * (des_host_register) are read in place by the upload.  The fields the last
+ * step has finished before its last pass (coordinates, velocity, force,
+ * temperature, plastic strain, strain rate, dpressure, edvoldt, ntmp) are
+ * downloaded while that pass runs, so with DES_ERR_DT they may already hold
+ * the step's values. */
 int  des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
                        des_step_report *report);
 

@@ -128,6 +128,45 @@ def test_step_host_round_trip(gpu):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_FP32])
+@pytest.mark.parametrize("nsteps", [1, 4])
+def test_step_host_overlapped_downloads(gpu, precision, nsteps):
+    """The fields finished before the last pass download on the second stream
+    while that pass runs in element chunks, each chunk's rows downloading
+    while the next computes: every field and dt equal upload/step/download,
+    with the loop-state mask and page-locked host arrays, and with the output
+    averaging switched on (it runs after the last pass)."""
+    c = case("plastic")
+    s0 = c.state_after(10 - nsteps)     # the last step forms dt (E-A runs in chunks there)
+    p = abi.Params.from_buffer_copy(c.params)
+    p.precision = precision
+    want = []
+    for avg in (0, 5):
+        # the same upload (and derived geometry) as des_gpu_step_host, then
+        # the steps as graphs and a plain download
+        dev = D.Device(c.mesh, p, device=0)
+        dev.set_averaging(avg)
+        dev.step_host(s0.copy(), 0, abi.F_STEP_STATE)
+        dev.step(nsteps)
+        want.append(dev.download(abi.State(c.mesh.nnode, c.mesh.nelem), abi.F_ALL))
+        dev.close()
+    for avg, pinned in ((0, False), (0, True), (5, True)):
+        dev = D.Device(c.mesh, p, device=0)
+        dev.set_averaging(avg)
+        b = s0.copy()
+        if pinned:
+            D.pin(b)
+        rep = dev.step_host(b, nsteps, abi.F_STEP_STATE)
+        if pinned:
+            D.unpin(b)
+        dev.close()
+        w = want[1 if avg else 0]
+        assert rep.status == 0 and rep.steps == s0.steps + nsteps
+        assert not diff_fields(b, w, COMPARED), (avg, pinned)
+        assert (b.time, b.dt, b.steps) == (w.time, w.dt, w.steps)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [abi.PREC_FP64, abi.PREC_FP32])
 def test_page_locked_host_buffers(gpu, precision):
     """Page-locked host arrays are read and written in place by the layout
     kernels (no staging copy); the results equal the staged path bit for bit."""
