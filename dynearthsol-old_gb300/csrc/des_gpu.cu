@@ -494,42 +494,50 @@ int prime(des_gpu *g)
     return DES_OK;
 }
 
-// passes N-A .. N-C of one step
-void launch_head(des_gpu *g, cudaEvent_t *ev)
+// pass k of N-A, E-B, N-B, E-C, N-C (0..4) of one step
+void launch_pass(des_gpu *g, int k)
 {
     const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
     cudaStream_t st = g->stream;
-    if (ev) cudaEventRecord(ev[0], st);
     if (g->prec == DES_PREC_FP32) {
         const DevF &f = g->f;
-        kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f);
-        if (ev) cudaEventRecord(ev[1], st);
-        if (g->closure && g->hF.rheol == 7)
-            kf_fe_b_nn<7><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
-        else if (g->closure)
-            kf_fe_b_nn<5><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
-        else
-            kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
-        if (ev) cudaEventRecord(ev[2], st);
-        kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f);
-        if (ev) cudaEventRecord(ev[3], st);
-        kf_fe_c<<<eb, kElemBlock, 0, st>>>(f);
-        if (ev) cudaEventRecord(ev[4], st);
-        kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f);
+        switch (k) {
+        case 0: kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f); break;
+        case 1:
+            if (g->closure && g->hF.rheol == 7)
+                kf_fe_b_nn<7><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
+            else if (g->closure)
+                kf_fe_b_nn<5><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
+            else
+                kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
+            break;
+        case 2: kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f); break;
+        case 3: kf_fe_c<<<eb, kElemBlock, 0, st>>>(f); break;
+        default: kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f); break;
+        }
     } else {
         const Dev &d = g->d;
-        k_fn_a<<<nb, kNodeBlock, 0, st>>>(d);
-        if (ev) cudaEventRecord(ev[1], st);
-        if (d.ret_log)
-            k_fe_b_t<true><<<eb, kElemBlock, 0, st>>>(d);
-        else
-            k_fe_b_t<false><<<eb, kElemBlock, 0, st>>>(d);
-        if (ev) cudaEventRecord(ev[2], st);
-        k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d);
-        if (ev) cudaEventRecord(ev[3], st);
-        k_fe_c<<<eb, kElemBlock, 0, st>>>(d);
-        if (ev) cudaEventRecord(ev[4], st);
-        k_fn_c<<<nb, kNodeBlock, 0, st>>>(d);
+        switch (k) {
+        case 0: k_fn_a<<<nb, kNodeBlock, 0, st>>>(d); break;
+        case 1:
+            if (d.ret_log)
+                k_fe_b_t<true><<<eb, kElemBlock, 0, st>>>(d);
+            else
+                k_fe_b_t<false><<<eb, kElemBlock, 0, st>>>(d);
+            break;
+        case 2: k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d); break;
+        case 3: k_fe_c<<<eb, kElemBlock, 0, st>>>(d); break;
+        default: k_fn_c<<<nb, kNodeBlock, 0, st>>>(d); break;
+        }
+    }
+}
+
+// passes N-A .. N-C of one step
+void launch_head(des_gpu *g, cudaEvent_t *ev)
+{
+    for (int k = 0; k < 5; ++k) {
+        if (ev) cudaEventRecord(ev[k], g->stream);
+        launch_pass(g, k);
     }
 }
 
@@ -1521,11 +1529,16 @@ void des_abi_sizes(long long out[5])
 // des_gpu_step_host downloads but does not upload them
 constexpr unsigned kStepOutputs =
     DES_F_FORCE | DES_F_NTMP | DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT | DES_F_TMP_RESULT;
-// fields a step has finished before its last pass: E-A writes none of them
-// (coordinates, velocity and temperature it only reads)
-constexpr unsigned kBeforeLastPass = DES_F_COORD | DES_F_COORD0 | DES_F_VEL | DES_F_FORCE |
-                                     DES_F_TEMPERATURE | DES_F_NTMP | DES_F_PLSTRAIN |
-                                     DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT;
+// fields that no pass after pass k (N-A, E-B, N-B, E-C, N-C) writes; E-A
+// writes none of them (coordinates, velocity and temperature it only reads)
+constexpr unsigned kFinishedAfterPass[5] = {
+    DES_F_TEMPERATURE | DES_F_COORD0,
+    DES_F_PLSTRAIN | DES_F_STRAIN_RATE | DES_F_DPRESSURE | DES_F_EDVOLDT,
+    DES_F_NTMP,
+    0,
+    DES_F_COORD | DES_F_VEL | DES_F_FORCE};
+constexpr unsigned kBeforeLastPass = kFinishedAfterPass[0] | kFinishedAfterPass[1] | kFinishedAfterPass[2] |
+                                     kFinishedAfterPass[3] | kFinishedAfterPass[4];
 
 // volume, shape derivatives and nodal masses from the device's coordinates
 // and temperature, the values update_mesh (dynearthsol.cxx:237-261) leaves
@@ -1576,20 +1589,23 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
     if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     if (nsteps > 1 && (rc = des_gpu_step(g, nsteps - 1, nullptr))) return rc;
     if ((rc = prime(g))) return rc;
-    std::vector<DownPart> early, late;
-    if ((rc = down_parts(g, host, mask & kBeforeLastPass, early)) ||
-        (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)))
+    std::vector<DownPart> all, late;
+    if ((rc = down_parts(g, host, mask, all)) || (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)))
         return rc;
     long long need = 0;
-    for (const DownPart &q : early) need += q.ncomp * q.rows;
-    for (const DownPart &q : late) need += q.ncomp * q.rows;
+    for (const DownPart &q : all) need += q.ncomp * q.rows;
     if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, need))) return rc;
     std::vector<DownPart> late_elem, late_node;
     for (const DownPart &q : late) (q.elem ? late_elem : late_node).push_back(q);
-    launch_head(g, nullptr);
-    DES_LAUNCH();
     long long off = 0;
-    rc = download_async(g, early, &off);
+    // each field downloads after the pass that finishes it
+    for (int k = 0; k < 5 && !rc; ++k) {
+        launch_pass(g, k);
+        rc = cuda_rc(cudaGetLastError());
+        std::vector<DownPart> done;
+        if (!rc) rc = down_parts(g, host, mask & kFinishedAfterPass[k], done);
+        if (!rc) rc = download_async(g, done, &off);
+    }
     // E-A in element chunks; each chunk's rows of the element fields go to
     // the host while the next chunk computes
     const int nb = blocks(g->nelem, kElemBlock), nchunk = std::min(kEaChunks, nb);
