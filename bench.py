@@ -460,6 +460,17 @@ def run_ours(args):
     achieved = alg[names[top]] * mesh.nelem / t_top / 1e9
     step_alg = (B_ELEM + B_NODE * r) * mesh.nelem
     step_gbs = step_alg / (ms / args.steps / 1e3) / 1e9
+    # FP64 pipe: DADD + DMUL + DFMA thread instructions per element of each
+    # pass in a step without the dt reduction (ncu instruction counters of the
+    # same passes on a 100x100x40 box of this physics), against GB300's 2 FP64
+    # instructions per clock per SM
+    fp64_ops = {"N-A": 23.1, "E-B": 66.0, "N-B": 5.4, "E-C": 105.0, "N-C": 19.7, "E-A": 430.8}
+    import torch
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    sm_hz = (clk.summary().get("sm_mhz") or 2070.0) * 1e6
+    fp64_peak = 2.0 * sms * sm_hz
+    fp64_top = fp64_ops[names[top]] * mesh.nelem / t_top
+    fp64_step = sum(fp64_ops.values()) * mesh.nelem / (ms / args.steps / 1e3)
 
     # the remesh trigger (bad_mesh_quality on the device), timed on the same state
     chk = abi.RemeshCheck(smallest_size=0.01, resolution=cfg.xlength / cfg.nx, zlength=cfg.zlength,
@@ -524,7 +535,13 @@ def run_ours(args):
                      "traffic": 417.0 * mesh.nelem if names[top] == "E-A" else None,
                      "peak_kind": hbm_kind,
                      "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,
-                     "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm},
+                     "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm,
+                     "fp64_pipe": {"kernel": names[top], "achieved": fp64_top, "peak": fp64_peak,
+                                   "unit": "FP64 inst/s", "frac": fp64_top / fp64_peak,
+                                   "ops_per_element": fp64_ops[names[top]],
+                                   "step_ops_per_element": sum(fp64_ops.values()),
+                                   "step_frac": fp64_step / fp64_peak,
+                                   "peak_kind": f"nominal: 2 per clock per SM x {sms} SMs at the sampled SM clock"}},
         "passes_ms_per_step": {n: t / prof_steps for n, t in zip(names, per_pass)},
         "forms": forms,
         "output_frame": output,
