@@ -673,6 +673,58 @@ __device__ __forceinline__ void spin(const R V[4][3], const R *dx, const R *dy, 
     for (int i = 0; i < 4; ++i) w5 += R(0.5) * (V[i][1] * dz[i] - V[i][2] * dy[i]);
 }
 
+// FP64: the spin (fields.cxx:483-504) and the strain rate (fields.cxx:193-241)
+// of the same velocities and gradients share their products V_i,a dN_i/db,
+// formed once here.  Both sum 0.5 (bracket) over the four nodes; scaling by
+// 0.5 is exact and commutes with rounding, so 0.5 times the sum of the
+// brackets equals the reference's sum bit for bit (for terms above the
+// subnormal range).
+__device__ __forceinline__ void spin_and_rate(const double V[4][3], const double *dx, const double *dy,
+                                              const double *dz, double &w3, double &w4, double &w5,
+                                              double D[6])
+{
+    D[0] = 0;
+    for (int i = 0; i < 4; ++i) D[0] += V[i][0] * dx[i];
+    D[1] = 0;
+    for (int i = 0; i < 4; ++i) D[1] += V[i][1] * dy[i];
+    D[2] = 0;
+    for (int i = 0; i < 4; ++i) D[2] += V[i][2] * dz[i];
+    double t3 = 0, t4 = 0, t5 = 0, u3 = 0, u4 = 0, u5 = 0;
+    for (int i = 0; i < 4; ++i) {
+        const double xy = V[i][0] * dy[i], yx = V[i][1] * dx[i];
+        const double xz = V[i][0] * dz[i], zx = V[i][2] * dx[i];
+        const double yz = V[i][1] * dz[i], zy = V[i][2] * dy[i];
+        t3 += xy + yx;
+        u3 += xy - yx;
+        t4 += xz + zx;
+        u4 += xz - zx;
+        t5 += yz + zy;
+        u5 += yz - zy;
+    }
+    D[3] = 0.5 * t3;
+    D[4] = 0.5 * t4;
+    D[5] = 0.5 * t5;
+    w3 = 0.5 * u3;
+    w4 = 0.5 * u4;
+    w5 = 0.5 * u5;
+}
+
+// fields.cxx:419-433 in FP64: the reference's 2 s_ab w products appear twice
+// each; 2 (s_ab w) is formed once per pair and the factor 2 applied to the
+// sum (exact, as above)
+__device__ __forceinline__ void jaumann64(double *s, double dt, double w3, double w4, double w5)
+{
+    const double p3 = s[3] * w3, p4 = s[4] * w4, p5 = s[5] * w5;
+    double inc[6];
+    inc[0] = 2.0 * (-p3 - p4);
+    inc[1] = 2.0 * (p3 - p5);
+    inc[2] = 2.0 * (p4 + p5);
+    inc[3] = s[0] * w3 - s[1] * w3 - s[4] * w5 - s[5] * w4;
+    inc[4] = s[0] * w4 - s[2] * w4 + s[3] * w5 - s[5] * w3;
+    inc[5] = s[1] * w5 - s[2] * w5 + s[3] * w4 + s[4] * w3;
+    for (int i = 0; i < 6; ++i) s[i] += dt * inc[i];
+}
+
 // fields.cxx:419-433
 template <class R>
 __device__ __forceinline__ void jaumann(R *s, R dt, R w3, R w4, R w5)

@@ -792,13 +792,12 @@ __global__ void k_init_stress(Dev d)
 
 // contributions for the next N-A pass from the current state: next strain
 // rate, tr(D) * volume, conduction vector
-__device__ __forceinline__ void next_step_contrib(const Dev &d, int e, int4 c, const double V[4][3],
-                                                  const double dx[4], const double dy[4],
-                                                  const double dz[4], double vol)
+// with the next step's strain rate D already formed
+__device__ __forceinline__ void next_step_contrib_d(const Dev &d, int e, int4 c, const double D[6],
+                                                    const double dx[4], const double dy[4],
+                                                    const double dz[4], double vol)
 {
     const size_t E = d.nelem;
-    double D[6];
-    strain_rate(V, dx, dy, dz, D);
     store6(d.srate_next, E, e, D);
     d.c_trdv[e] = tr3(D) * vol;
     if (d.K->thermal) {
@@ -807,6 +806,15 @@ __device__ __forceinline__ void next_step_contrib(const Dev &d, int e, int4 c, c
         conduction(dx, dy, dz, Tn, d.K->M.mix[d.mix[e]].k * vol, tr);
         for (int i = 0; i < 4; ++i) d.tmp[i * E + e] = tr[i];
     }
+}
+
+__device__ __forceinline__ void next_step_contrib(const Dev &d, int e, int4 c, const double V[4][3],
+                                                  const double dx[4], const double dy[4],
+                                                  const double dz[4], double vol)
+{
+    double D[6];
+    strain_rate(V, dx, dy, dz, D);
+    next_step_contrib_d(d, e, c, D, dx, dy, dz, vol);
 }
 
 __global__ void k_prime(Dev d)
@@ -1029,18 +1037,19 @@ __global__ void k_fe_a(Dev d, int e0, unsigned nblocks)
         }
         double V[4][3];
         load_vel4(d, c, V);
+        double w3, w4, w5, D[6];
+        spin_and_rate(V, dx, dy, dz, w3, w4, w5, D);
         if (K.rheol & 1) {
-            double w3, w4, w5, s[6];
-            spin(V, dx, dy, dz, w3, w4, w5);
+            double s[6];
             const double dt = d.clk->dt;
             load6(d.stress, E, e, s);
-            jaumann(s, dt, w3, w4, w5);
+            jaumann64(s, dt, w3, w4, w5);
             store6(d.stress, E, e, s);
             load6(d.strain, E, e, s);
-            jaumann(s, dt, w3, w4, w5);
+            jaumann64(s, dt, w3, w4, w5);
             store6(d.strain, E, e, s);
         }
-        next_step_contrib(d, e, c, V, dx, dy, dz, vol);
+        next_step_contrib_d(d, e, c, D, dx, dy, dz, vol);
         if (dt_step) {
             minh = min_height(X, vol);
             dtd = 0.5 * minh * minh / K.therm_diff_max;
