@@ -296,18 +296,22 @@ int build_consts(des_gpu *g)
         for (int j = 0; j < DES_NBDRY; ++j)
             for (int k = 0; k < 3; ++k) K.edge[i][j][k] = p.edge_vectors[i][j][k];
     }
-    // apply_stress_bcs (bc.cxx:503-595) does something only for these cases
-    g->stress_bcs = false;
+    // apply_stress_bcs (bc.cxx:503-595): the sides whose facets carry a
+    // traction, and the elastic foundation (both only with gravity)
+    K.stress_bc_sides = 0;
     if (p.gravity != 0) {
         for (int i = 0; i < DES_NBDRY; ++i) {
             int t = p.vbc_types[i];
             if (t != 0 && t != 2 && t != 4) continue;
             if (i == 4 && !p.has_winkler_foundation) continue;
             if (i == 5 && !p.has_water_loading) continue;
-            if (g->bfacets_count[i] > 0) g->stress_bcs = true;
+            if (g->bfacets_count[i] > 0) K.stress_bc_sides |= 1u << i;
         }
     }
-    if (p.has_elastic_foundation) g->stress_bcs = true;
+    K.elastic_foundation = (p.gravity != 0 && p.has_elastic_foundation) ? 1 : 0;
+    K.elastic_foundation_constant = p.elastic_foundation_constant;
+    K.winkler_delta_rho = p.winkler_delta_rho;
+    g->stress_bcs = K.stress_bc_sides != 0 || K.elastic_foundation;
     if (cudaMemcpyAsync(g->dK, &g->hK, sizeof(Consts), cudaMemcpyHostToDevice, g->stream) !=
         cudaSuccess)
         return DES_ERR_CUDA;
@@ -513,7 +517,11 @@ void launch_pass(des_gpu *g, int k)
             break;
         case 2: kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f); break;
         case 3: kf_fe_c<<<eb, kElemBlock, 0, st>>>(f); break;
-        default: kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f); break;
+        default:
+            if (g->hK.stress_bc_sides && g->d.sbc.nbf > 0)
+                k_stress_bc_facets<<<blocks(g->d.sbc.nbf, 128), 128, 0, st>>>(g->d);
+            kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f);
+            break;
         }
     } else {
         const Dev &d = g->d;
@@ -527,7 +535,11 @@ void launch_pass(des_gpu *g, int k)
             break;
         case 2: k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d); break;
         case 3: k_fe_c<<<eb, kElemBlock, 0, st>>>(d); break;
-        default: k_fn_c<<<nb, kNodeBlock, 0, st>>>(d); break;
+        default:
+            if (g->hK.stress_bc_sides && d.sbc.nbf > 0)
+                k_stress_bc_facets<<<blocks(d.sbc.nbf, 128), 128, 0, st>>>(d);
+            k_fn_c<<<nb, kNodeBlock, 0, st>>>(d);
+            break;
         }
     }
 }
@@ -781,6 +793,52 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     g->staging_elems = std::max<long long>(g->staging_elems, 3LL * (long long)N < (1LL << 25) ? 3LL * (long long)N : (1LL << 25));
     if ((rc = dev_alloc(g, &g->staging, (size_t)g->staging_elems))) return fail(rc);
 
+    // apply_stress_bcs: every boundary facet, and each node's facets in the
+    // order bc.cxx:568-590 subtracts them (side by side, facets in bfacets
+    // order)
+    {
+        static const int kFacetHost[4][3] = {{1, 2, 3}, {0, 3, 2}, {0, 1, 3}, {0, 2, 1}};   // constants.hpp:61-67
+        int nbf = 0;
+        for (int i = 0; i < DES_NBDRY; ++i) nbf += topo->bfacets_count[i];
+        std::vector<int> belem((size_t)nbf), off(N + 1, 0), nodes(3 * (size_t)nbf);
+        std::vector<unsigned char> bsf((size_t)nbf);
+        int k = 0;
+        for (int i = 0; i < DES_NBDRY; ++i)
+            for (int j = 0; j < topo->bfacets_count[i]; ++j, ++k) {
+                const int e = topo->bfacets[i][2 * j], f = topo->bfacets[i][2 * j + 1];
+                belem[k] = e;
+                bsf[k] = (unsigned char)((i << 2) | f);
+                for (int q = 0; q < 3; ++q) {
+                    nodes[3 * (size_t)k + q] = m->connectivity[4 * (size_t)e + kFacetHost[f][q]];
+                    ++off[nodes[3 * (size_t)k + q] + 1];
+                }
+            }
+        for (size_t n = 0; n < N; ++n) off[n + 1] += off[n];
+        std::vector<int> fill(off.begin(), off.end() - 1), nf((size_t)off[N]);
+        for (int q = 0; q < 3 * nbf; ++q) nf[(size_t)fill[nodes[q]]++] = q / 3;
+        int *d_elem, *d_off, *d_nf;
+        unsigned char *d_sf;
+        double *d_val;
+        if ((rc = dev_alloc(g, &d_elem, (size_t)nbf)) || (rc = dev_alloc(g, &d_sf, (size_t)nbf)) ||
+            (rc = dev_alloc(g, &d_val, 3 * (size_t)nbf)) || (rc = dev_alloc(g, &d_off, N + 1)) ||
+            (rc = dev_alloc(g, &d_nf, (size_t)off[N])))
+            return fail(rc);
+        if (cudaMemcpy(d_elem, belem.data(), sizeof(int) * nbf, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(d_sf, bsf.data(), (size_t)nbf, cudaMemcpyHostToDevice) ||
+            cudaMemcpy(d_off, off.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice) ||
+            cudaMemcpy(d_nf, nf.data(), sizeof(int) * nf.size(), cudaMemcpyHostToDevice))
+            return fail(DES_ERR_CUDA);
+        StressBc sb;
+        sb.nbf = nbf;
+        sb.elem = d_elem;
+        sb.side_f = d_sf;
+        sb.val = d_val;
+        sb.node_off = d_off;
+        sb.node_facet = d_nf;
+        g->d.sbc = sb;
+        g->f.sbc = sb;
+    }
+
     std::vector<unsigned> ent(4 * E);
     for (size_t q = 0; q < 4 * E; ++q)
         ent[q] = ((unsigned)topo->support_elems[q] << 2) | (unsigned)topo->support_slots[q];
@@ -831,12 +889,11 @@ int des_gpu_set_params(des_gpu *g, const des_params *p)
     g->primed = false;
     rc = build_consts(g);
     if (rc) return rc;
-    if (g->closure) {
-        // the stress pass with the closure is specialised on the rheology
-        if (g->graph) cudaGraphExecDestroy(g->graph);
-        g->graph = nullptr;
-        if (g->hF.rheol != 5 && g->hF.rheol != 7) g->closure = false;
-    }
+    // the captured step depends on the rheology (closure) and on whether
+    // boundary tractions apply
+    if (g->graph) cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+    if (g->closure && g->hF.rheol != 5 && g->hF.rheol != 7) g->closure = false;
     return DES_OK;
 }
 
@@ -861,7 +918,11 @@ int des_gpu_set_elemmarkers(des_gpu *g, const int *elemmarkers)
 }
 
 long long des_gpu_device_bytes(const des_gpu *g) { return g ? g->bytes : 0; }
-int des_gpu_kernels_per_step(const des_gpu *g) { return g ? kStepKernels : 0; }
+int des_gpu_kernels_per_step(const des_gpu *g)
+{
+    if (!g) return 0;
+    return kStepKernels + ((g->hK.stress_bc_sides && g->d.sbc.nbf > 0) ? 1 : 0);
+}
 
 int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
 {
@@ -1412,7 +1473,7 @@ int des_gpu_set_closure(des_gpu *g, const des_mlp *net)
 int des_gpu_log_returns(des_gpu *g, int nsteps, float *records, long long capacity, long long *count)
 {
     if (!g || nsteps < 1 || capacity < 1 || !records || !count) return DES_ERR_ARG;
-    if (g->prec != DES_PREC_FP64 || g->stress_bcs) return DES_ERR_UNSUPPORTED;
+    if (g->prec != DES_PREC_FP64) return DES_ERR_UNSUPPORTED;
     if (int rc = prime(g)) return rc;
     float *buf = nullptr;
     if (cudaMalloc(&buf, sizeof(float) * kRetRecord * (size_t)capacity) != cudaSuccess) return DES_ERR_NOMEM;
@@ -1441,7 +1502,6 @@ int des_gpu_log_returns(des_gpu *g, int nsteps, float *records, long long capaci
 int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)
 {
     if (!g || nsteps < 0) return DES_ERR_ARG;
-    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     if (int rc = prime(g)) return rc;
     if (!g->graph) {
         int rc = capture_step_graph(g);
@@ -1460,7 +1520,6 @@ int des_gpu_step(des_gpu *g, int nsteps, des_step_report *report)
 int des_gpu_time_steps(des_gpu *g, int nsteps, double *ms)
 {
     if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
-    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     if (int rc = prime(g)) return rc;
     if (!g->graph) {
         int rc = capture_step_graph(g);
@@ -1485,7 +1544,6 @@ int des_gpu_time_steps(des_gpu *g, int nsteps, double *ms)
 int des_gpu_profile_steps(des_gpu *g, int nsteps, double ms[6])
 {
     if (!g || nsteps < 0 || !ms) return DES_ERR_ARG;
-    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     if (int rc = prime(g)) return rc;
     cudaEvent_t ev[7];
     for (int i = 0; i < 7; ++i) DES_CUDA(cudaEventCreate(&ev[i]));
@@ -1586,7 +1644,6 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
     // every step but the last as the graph; the last as its passes, so that
     // the fields finished before E-A download on the copy stream while E-A
     // runs (the host link is the bound of this entry point)
-    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     if (nsteps > 1 && (rc = des_gpu_step(g, nsteps - 1, nullptr))) return rc;
     if ((rc = prime(g))) return rc;
     std::vector<DownPart> all, late;
@@ -1754,8 +1811,9 @@ int des_gpu_update_force(des_gpu *g)
 {
     int rc = begin_fn64(g);
     if (rc) return rc;
-    if (g->stress_bcs) return DES_ERR_UNSUPPORTED;
     k_force_elem<<<ELEM_GRID(g)>>>(g->d);
+    if (g->hK.stress_bc_sides && g->d.sbc.nbf > 0)
+        k_stress_bc_facets<<<blocks(g->d.sbc.nbf, 128), 128, 0, g->stream>>>(g->d);
     k_force_node<<<NODE_GRID(g)>>>(g->d, g->hK.is_qs);
     return finish(g);
 }

@@ -25,6 +25,9 @@ struct Consts {
     double gravity, damping_factor, surface_temperature, dt_fraction, fixed_dt;
     double inertial_scaling, max_vbc_val, therm_diff_max, zlength, rho0_0;
     double compensation_pressure;
+    double winkler_delta_rho, elastic_foundation_constant;
+    unsigned stress_bc_sides;   // sides whose facets carry apply_stress_bcs' tractions
+    int elastic_foundation;     // the bottom restoring force of apply_stress_bcs
     int damping_option, is_qs, thermal, rheol;
     int vbc_types[10];
     double vbc_values[10];
@@ -40,6 +43,18 @@ struct Clock {
     unsigned long long ql, eig;
     unsigned long long nlog;                    // return-map records seen (logging launches)
     unsigned long long nn_cand, nn_accept, fp64_returns;   // learned-closure counters
+};
+
+// The boundary facets of apply_stress_bcs (bc.cxx:503-595) and, for every
+// node, the facets it belongs to in the order the reference subtracts their
+// tractions (side by side, facets in bfacets order).
+struct StressBc {
+    int nbf;
+    const int *elem;                // [nbf] element of each facet
+    const unsigned char *side_f;    // [nbf] side << 2 | facet of the element
+    double *val;                    // [3][nbf] traction p n / 3 on each of its nodes
+    const int *node_off;            // [nnode + 1]
+    const int *node_facet;          // facet indices
 };
 
 struct Dev {
@@ -60,6 +75,7 @@ struct Dev {
     Clock *clk;
     float *ret_log;                  // return-map records (logging launches only)
     long long ret_cap;
+    StressBc sbc;
 };
 
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
@@ -595,6 +611,69 @@ __global__ void k_force_elem(Dev d)
     force_elem_body(d, e, d.conn[e], s);
 }
 
+// node j of facet f of a tetrahedron (constants.hpp:61-67: {1,2,3},
+// {0,3,2}, {0,1,3}, {0,2,1}), two bits per entry
+__device__ __forceinline__ int facet_node(int f, int j)
+{
+    constexpr unsigned kPacked = (1u << 0) | (2u << 2) | (3u << 4) | (0u << 6) | (3u << 8) | (2u << 10) |
+                                 (0u << 12) | (1u << 14) | (3u << 16) | (0u << 18) | (2u << 20) | (1u << 22);
+    return (kPacked >> (2 * (3 * f + j))) & 3u;
+}
+
+// bc.cxx:528-566 for one boundary facet: its outward normal n with the
+// facet's area as length (bc.cxx:15-36), the pressure p of its side and the
+// traction p n / 3 each of its three nodes receives
+__global__ void k_stress_bc_facets(Dev d)
+{
+    const int k = gtid();
+    const StressBc &b = d.sbc;
+    if (k >= b.nbf) return;
+    const Consts &K = *d.K;
+    const int side = b.side_f[k] >> 2, f = b.side_f[k] & 3;
+    if (!(K.stress_bc_sides & (1u << side))) return;
+    const int e = b.elem[k];
+    const int4 c4 = d.conn[e];
+    auto pick = [&](int i) { return i == 0 ? c4.x : i == 1 ? c4.y : i == 2 ? c4.z : c4.w; };
+    const int n0 = pick(facet_node(f, 0)), n1 = pick(facet_node(f, 1)), n2 = pick(facet_node(f, 2));
+    const double v01[3] = {d.x[n1] - d.x[n0], d.y[n1] - d.y[n0], d.z[n1] - d.z[n0]};
+    const double v02[3] = {d.x[n2] - d.x[n0], d.y[n2] - d.y[n0], d.z[n2] - d.z[n0]};
+    double normal[3];
+    normal[0] = (v01[1] * v02[2] - v01[2] * v02[1]) / 2;
+    normal[1] = (v01[2] * v02[0] - v01[0] * v02[2]) / 2;
+    normal[2] = (v01[0] * v02[1] - v01[1] * v02[0]) / 2;
+    const double zcenter = (d.z[n0] + d.z[n1] + d.z[n2]) / 3;
+    double p;
+    if (side == 4) {
+        // Winkler foundation under the bottom
+        double Tn[4];
+        load_nodal4(d.T, c4, Tn);
+        const double rho = mat_rho(K.M, K.M.mix[d.mix[e]], elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3]));
+        p = K.compensation_pressure - (rho + K.winkler_delta_rho) * K.gravity * (zcenter + K.zlength);
+    } else if (side == 5) {
+        // water loading on the surface below sea level (0)
+        p = 0;
+        if (zcenter < 0) p = 1030 * K.gravity * (0 - zcenter);
+    } else {
+        p = K.rho0_0 * K.gravity * (-zcenter);    // ref_pressure (matprops.cxx:523-535)
+    }
+    for (int j = 0; j < 3; ++j) b.val[j * b.nbf + k] = p * normal[j] / 3;
+}
+
+// bc.cxx:568-590 for node n after update_force's gather: the tractions of its
+// boundary facets, then the elastic foundation's restoring force on the bottom
+__device__ __forceinline__ void stress_bc_node(const Consts &K, const StressBc &b, int n, unsigned flag,
+                                               double z, double z0, double f[3])
+{
+    if (K.stress_bc_sides && (flag & kBoundAny)) {
+        for (int q = b.node_off[n]; q < b.node_off[n + 1]; ++q) {
+            const int k = b.node_facet[q];
+            if (!(K.stress_bc_sides & (1u << (b.side_f[k] >> 2)))) continue;
+            for (int j = 0; j < 3; ++j) f[j] -= b.val[j * b.nbf + k];
+        }
+    }
+    if (K.elastic_foundation && (flag & kBoundZ0)) f[2] -= K.elastic_foundation_constant * (z - z0);
+}
+
 // fields.cxx:351-365 + apply_damping (fields.cxx:250-309)
 __device__ __forceinline__ void force_gather(const Dev &d, int n, double f[3])
 {
@@ -614,6 +693,7 @@ __global__ void k_force_node(Dev d, int damping)
     if (n >= d.nnode) return;
     double f[3];
     force_gather(d, n, f);
+    stress_bc_node(*d.K, d.sbc, n, d.bcflag[n], d.z[n], d.z0[n], f);
     if (damping) {
         const Consts &K = *d.K;
         f[0] = damp(K, f[0], d.vx[n]);
@@ -980,6 +1060,7 @@ __global__ void k_fn_c(Dev d)
     const double dt = d.clk->dt;
     double f[3];
     force_gather(d, n, f);
+    stress_bc_node(K, d.sbc, n, d.bcflag[n], d.z[n], d.z0[n], f);
     double v[3] = {d.vx[n], d.vy[n], d.vz[n]};
     if (K.is_qs) {
         f[0] = damp(K, f[0], v[0]);

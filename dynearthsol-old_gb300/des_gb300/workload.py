@@ -152,6 +152,9 @@ def make_params(cfg, precision=abi.PREC_FP64):
     p.max_vbc_val = find_max_vbc(types, vals)
     for k, v in cfg.extra.get("params", {}).items():
         setattr(p, k, v)
+    # Variables::compensation_pressure as init() sets it (ic.cxx:131,
+    # ref_pressure of the bottom), for a device given a state without init
+    p.compensation_pressure = p.rho0.v[0] * p.gravity * p.zlength if p.gravity != 0 else 0.0
     p.precision = precision
     return p
 

@@ -38,6 +38,76 @@ def layered_config(nx=6, ny=5, nz=6):
     return cfg
 
 
+def _variant(name, nx=6, ny=5, nz=3, base="1", rheology=None, params=None, mats=None, vbc=None,
+             **cfg_kw):
+    cfg = W.scaled(W.CONFIGS[base], nx, ny, nz, name=f"opt_{name}_{nx}x{ny}x{nz}")
+    if rheology:
+        cfg.rheology = rheology
+    for k, v in cfg_kw.items():
+        setattr(cfg, k, v)
+    extra = dict(cfg.extra)
+    if params:
+        extra["params"] = dict(extra.get("params", {}), **params)
+    if mats:
+        extra["mats"] = dict(extra.get("mats", {}), **mats)
+    if vbc:
+        extra["vbc_types"], extra["vbc_values"] = vbc
+    cfg.extra = extra
+    return cfg
+
+
+_YR = 365.2425 * 86400
+# Options of the loop that the five workloads do not exercise (each on a small
+# box of config 1's physics unless stated): the other rheologies, damping
+# options, a fixed dt, the dynamic (not quasi-static) mode, no thermal
+# diffusion, no gravity, the other velocity boundary types of the x, y and z
+# sides (bc.cxx:182-500), the largest material count and a one-hex mesh.
+OPTION_VARIANTS = {
+    "elastic": _variant("elastic", params=dict(rheol_type=1)),
+    # a viscosity the explicit step can carry (eta / dt near the shear modulus)
+    "viscous": _variant("viscous", base="3", params=dict(rheol_type=2, visc_min=1e17, visc_max=3e17)),
+    "maxwell": _variant("maxwell", base="3", params=dict(rheol_type=3)),
+    "damping0": _variant("damping0", params=dict(damping_option=0)),
+    "damping2": _variant("damping2", params=dict(damping_option=2)),
+    "damping3": _variant("damping3", params=dict(damping_option=3)),
+    "fixed_dt": _variant("fixed_dt", params=dict(fixed_dt=1e7)),
+    "dynamic": _variant("dynamic", params=dict(is_quasi_static=0)),
+    "no_thermal": _variant("no_thermal", params=dict(has_thermal_diffusion=0)),
+    "no_gravity": _variant("no_gravity", params=dict(gravity=0.0)),
+    "vbc_a": _variant("vbc_a", vbc=([3, 5, 2, 4, 1, 0, 0, 0, 0, 0],
+                                    [-0.01 / _YR, 0.02 / _YR, 0.0, 0.005 / _YR, 0.0, 0.0, 0, 0, 0, 0])),
+    "vbc_b": _variant("vbc_b", vbc=([7, 7, 7, 3, 3, 2, 0, 0, 0, 0],
+                                    [-0.01 / _YR, 0.01 / _YR, 0.003 / _YR, -0.002 / _YR, 0.0, 0.0, 0, 0, 0, 0])),
+    # apply_stress_bcs (bc.cxx:503-595): lithostatic tractions on sides whose
+    # normal velocity is free, the Winkler foundation under a free bottom, water
+    # loading on the surface, the elastic foundation
+    "free_x0": _variant("free_x0", vbc=([0, 1, 1, 1, 1, 0, 0, 0, 0, 0],
+                                        [0.0, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    "winkler": _variant("winkler", params=dict(has_winkler_foundation=1, winkler_delta_rho=100.0),
+                        vbc=([1, 1, 1, 1, 0, 0, 0, 0, 0, 0],
+                             [-0.01 / _YR, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    "water": _variant("water", params=dict(has_water_loading=1)),
+    # (cohesion high enough that nothing yields: the reference's fast-math
+    # eigen-solver and the strict restatement differ by rounding on returns)
+    "elastic_fnd": _variant("elastic_fnd", params=dict(has_elastic_foundation=1,
+                                                        elastic_foundation_constant=1e11),
+                            mats=dict(cohesion0=[1e9], cohesion1=[1e9]),
+                            vbc=([1, 1, 1, 1, 2, 0, 0, 0, 0, 0],
+                                 [-0.01 / _YR, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    "mats16": _variant("mats16", nz=6, nlayers=16,
+                       layer_rho0=tuple(2700.0 + 40.0 * k for k in range(16)),
+                       layer_depths=tuple((k + 1) / 16 for k in range(15)),
+                       mats=dict(shear_modulus=[25e9 + 1e9 * k for k in range(16)],
+                                 bulk_modulus=[100e9 + 3e9 * k for k in range(16)],
+                                 therm_cond=[2.5 + 0.1 * k for k in range(16)],
+                                 cohesion0=[30e6 + 2e6 * k for k in range(16)])),
+    "one_hex": _variant("one_hex", nx=1, ny=1, nz=1),
+}
+# variants whose arithmetic includes pow/exp (CUDA's differ from the host
+# libm by an ulp): a per-step tolerance instead of bit-identity
+OPTION_TRANSCENDENTAL = {"viscous", "maxwell"}
+
+
 def phase_config(nx=8, ny=6, nz=6):
     """Three layers whose materials differ in density, moduli, conductivity,
     heat capacity and cohesion, so a phase change moves every mixed property;

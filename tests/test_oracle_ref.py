@@ -161,3 +161,22 @@ def test_post_remesh_sequence_and_steps_bit_exact():
     r2.step(b2, 20)
     assert not diff_fields(a2, b2, COMPARED + ["coord0"])
     assert (a2.time, a2.dt, a2.steps) == (b2.time, b2.dt, b2.steps)
+
+
+@pytest.mark.parametrize("name", sorted(__import__("helpers").OPTION_VARIANTS))
+def test_option_variants_50_steps_bit_exact(name):
+    """The options the five workloads leave out (other rheologies, damping
+    options, fixed dt, dynamic mode, no thermal diffusion, no gravity, other
+    velocity boundary types, 16 materials, one hex): init() and 50 steps of
+    the restatement against the reference's own functions."""
+    from helpers import OPTION_VARIANTS
+    c, r = both(OPTION_VARIANTS[name])
+    a = W.new_state(c.mesh, c.T, c.pls)
+    b = W.new_state(c.mesh, c.T, c.pls)
+    c.oracle.init_fields(a)
+    r.init_fields(b)
+    assert not diff_fields(a, b) and a.dt == b.dt
+    c.oracle.step(a, 50)
+    r.step(b, 50)
+    assert not diff_fields(a, b), diff_fields(a, b)
+    assert (a.time, a.dt, a.steps) == (b.time, b.dt, b.steps)
