@@ -1,10 +1,12 @@
-// The learned return-map closure inside the FP32 stress pass (E-B).
+// The FP32 form's elasto-(visco-)plastic stress pass (E-B) and the learned
+// return-map closure inside it.
 //
 // For the elasto-plastic rheologies the reference computes the principal
 // stresses of the elastic trial with dsyevh3 and returns the trial to the
 // Mohr-Coulomb surface (rheology.cxx:180-240); the FP32 form does that in
-// FP64 for every element the cheap elastic bound cannot clear.  With a
-// closure set, the pass sorts those elements per CTA:
+// FP64 for every element the cheap elastic bounds cannot clear.  Those
+// elements are listed (E-B1) and returned by a dense pass (E-B3).  With a
+// closure set, a pass in between (E-B2) sorts the listed elements:
 //
 //   network candidates  the FP32 principal values of the trial say "shear
 //                       return, clearly": fs < -tol S and h < -tol S
@@ -12,15 +14,13 @@
 //                       or corner branches, inputs outside the training
 //                       envelope)
 //
-// Candidates are compacted into 16-row tiles and evaluated by the MLP on the
+// Candidates are packed into 16-row tiles and evaluated by the MLP on the
 // tensor cores.  Each prediction is then judged in FP32: the predicted
 // stress must lie on the yield surface, |fs(sigma) - 2 sqrt(anphi) hardn
 // alam| <= tol S (the hardening term is the residual the reference's own
 // return leaves), inside the tensile cutoff, with a positive plastic-strain
 // increment; for rh_evp the Maxwell/plastic choice must also be clear.
-// Rejected candidates join the exact queue, and the exact queue is
-// compacted onto the first threads of the CTA, which run the FP64 return
-// map, so that the FP64 work is not spread over every warp.
+// Rejected candidates join the exact list.
 //
 // Network input (14; 8 used): four quantities, functions of the old stress,
 // the strain increment and the plastic strain,
@@ -43,21 +43,6 @@
 #include "des_mlp.cuh"
 
 namespace des {
-
-constexpr int kNnBlock = 128;
-
-struct NnSmem {
-    __nv_bfloat16 w1[kMlpHid * kMlpIn], w2[kMlpHid * kMlpHid], w3[kMlpOut * kMlpHid];
-    float b1[kMlpHid], b2[kMlpHid], b3[kMlpOut];
-    __nv_bfloat16 x[kNnBlock * kMlpIn];
-    __nv_bfloat16 h1[kNnBlock / 32][16 * kHStride], h2[kNnBlock / 32][16 * kHStride];
-    float y[kNnBlock * kMlpOut];
-    float so[6][kNnBlock], de[6][kNnBlock];      // inputs of the exact return map
-    float res[6][kNnBlock];                      // its outputs
-    double resd[kNnBlock];
-    int queue[kNnBlock];
-    int wcount[kNnBlock / 32];
-};
 
 // FP32 plastic properties with the dilation factor and the hardening slope
 // (matprops.cxx:646-704)
@@ -142,67 +127,217 @@ struct NnCand {
     float alam, S, cf, anphi, hardn, ft_shift;
 };
 
-// kind: 0 = done (elastic), 1 = network candidate, 2 = exact FP64 return map
+// ---- the elasto-(visco-)plastic stress pass as three dense kernels -------
+//
+// E-B1 (kf_fe_b_ep) corrects the strain rate, updates the strain and forms
+// the elastic trial of every element, and finishes every element the FP32
+// bounds prove elastic; each other element goes to the pending list.  With a
+// closure, E-B2 (kf_nn_list) takes the pending list 32 entries per warp,
+// evaluates the network on the candidates among them in full 16-row tiles
+// (the weights staged once per CTA) and judges each prediction; the rest join
+// the exact list.  E-B3 (kf_exact_list) runs the FP64 return map on the
+// pending list (no closure) or the exact list, with every lane busy.  The
+// later kernels recompute an element's trial from what E-B1 left (the old
+// stress still in place, the corrected strain rate in srate) with the same
+// FP32 arithmetic, so the result does not depend on which kernel finishes an
+// element.
+
+// one element's stress-update inputs
+struct FTrial {
+    float so[6], de[6], s[6], sv[6];   // old stress, increment, elastic trial, Maxwell stress (rh_evp)
+    float visc, dt;
+    double pls, s0;
+    int4 c;
+    int mix;
+};
+
 template <int RHEOL>
-__global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__restrict__ net)
+__device__ __forceinline__ void f_trial_from_state(const DevF &d, int e, FTrial &q)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    NnSmem &S = *reinterpret_cast<NnSmem *>(smem_raw);
-    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-    const int e = blockIdx.x * kNnBlock + tid;
-    if (e == 0) d.clk->mass_valid = 1;
-    const bool live = e < d.nelem;
     const size_t E = d.nelem;
     const ConstsF &F = *d.F;
-    const float tol = net->tol;
+    q.c = d.conn[e];
+    q.mix = d.mix[e];
+    const MixF &xf = F.mix[q.mix];
+    float edot[6];
+    f_load6(d.stress, E, e, q.so);
+    f_load6(d.srate, E, e, edot);
+    q.pls = d.pls[e];
+    q.s0 = d.s0[e];
+    q.dt = (float)d.clk->dt;
+    for (int i = 0; i < 6; ++i) {
+        q.de[i] = edot[i] * q.dt;
+        q.s[i] = q.so[i];
+    }
+    elastic(xf.bulkm, xf.shearm, q.de, q.s);
+    q.visc = 0.f;
+    if (RHEOL == 7) {
+        q.visc = f_visc(F, xf, f_elem_T(d, q.c), edot);
+        const float dv = (float)(d.vol[e] / d.vol_old[e] - 1);
+        for (int i = 0; i < 6; ++i) q.sv[i] = q.so[i];
+        maxwell(xf.bulkm, xf.shearm, q.visc, q.dt, dv, q.de, q.sv);
+    }
+}
 
-    int kind = 0;
-    float so[6], de[6];      // old stress and strain increment (deviation form)
-    float s[6], sv[6];       // trial, Maxwell stress (rh_evp)
-    float visc = 0.f, dpls = 0.f, dt = 0.f;
-    double pls = 0.0, s0 = 0.0;
-    NnCand cd = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    float raw[kMlpIn];
-    int mixid = 0;
+// the element's new stress from the plastic candidate sp (rheology.cxx:578-598,
+// 628-638 for rh_evp), plastic strain, dpressure and its volume-weighted share
+template <int RHEOL>
+__device__ __forceinline__ void f_finish(const DevF &d, int e, const FTrial &q, const float sp[6], double depls,
+                                         bool from_network)
+{
+    const size_t E = d.nelem;
+    bool plastic = true;
+    if (RHEOL == 7) {
+        plastic = from_network ? second_invariant2(q.sv) >= second_invariant2(sp)
+                               : !f_viscous_wins(d.F->mix[q.mix], q.so, q.de, q.sv, sp, depls, q.dt, q.visc);
+    }
+    float s[6];
+    if (plastic) {
+        for (int i = 0; i < 6; ++i) s[i] = sp[i];
+        d.pls[e] = q.pls + depls;
+        d.dpls[e] = (float)depls;
+    } else {
+        for (int i = 0; i < 6; ++i) s[i] = q.sv[i];
+    }
+    const float dpv = tr3(s) - tr3(q.so);
+    f_store6(d.stress, E, e, s);
+    d.dp[e] = dpv;
+    d.tmp_sg[e] = dpv * d.c_vol[e];
+}
+
+// appends e (where take) to list with one atomic per warp; every lane of the
+// warp calls it
+__device__ __forceinline__ void list_append(unsigned *count, int *list, bool take, int e)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, take);
+    if (!m) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (take) list[base + __popc(m & ((1u << lane) - 1u))] = e;
+}
+
+// E-B1
+template <int RHEOL>
+__global__ void kf_fe_b_ep(DevF d)
+{
+    const int e = gtid();
+    if (e == 0) d.clk->mass_valid = 1;
+    const bool live = e < d.nelem;
+    bool pending = false;
     if (live) {
-        int4 c = d.conn[e];
-        mixid = d.mix[e];
-        const MixF &xf = F.mix[mixid];
-        float edv = (d.ntmp[c.x] + d.ntmp[c.y] + d.ntmp[c.z] + d.ntmp[c.w]) * 0.25f;
+        const size_t E = d.nelem;
+        const ConstsF &F = *d.F;
+        const int4 c = d.conn[e];
+        const MixF &xf = F.mix[d.mix[e]];
+        const float edv = (d.ntmp[c.x] + d.ntmp[c.y] + d.ntmp[c.z] + d.ntmp[c.w]) * 0.25f;
         d.edvoldt[e] = edv;
-        float es[6], edot[6];
+        float so[6], es[6], edot[6];
         f_load6(d.stress, E, e, so);
         f_load6(d.strain, E, e, es);
         f_load6(d.srate_next, E, e, edot);
-        pls = d.pls[e];
-        s0 = d.s0[e];
-        dpls = d.dpls[e];
-        dt = (float)d.clk->dt;
-        float div = tr3(edot);
+        const float dt = (float)d.clk->dt;
+        const float div = tr3(edot);
         for (int i = 0; i < 3; ++i) edot[i] += (edv - div) * (1.f / 3.f);
+        float de[6], st[6];
         for (int i = 0; i < 6; ++i) {
             es[i] += edot[i] * dt;
             de[i] = edot[i] * dt;
-            s[i] = so[i];
+            st[i] = so[i];
         }
         f_store6(d.strain, E, e, es);
         f_store6(d.srate, E, e, edot);
-        const float Te = f_elem_T(d, c);
-        if (RHEOL == 7) {
-            visc = f_visc(F, xf, Te, edot);
-            float dv = (float)(d.vol[e] / d.vol_old[e] - 1);
-            for (int i = 0; i < 6; ++i) sv[i] = so[i];
-            maxwell(xf.bulkm, xf.shearm, visc, dt, dv, de, sv);
+        elastic(xf.bulkm, xf.shearm, de, st);
+        const float s0f = (float)d.s0[e];
+        float amc, anphi, ten_max;
+        f_plastic_props(F, xf, (float)d.pls[e], amc, anphi, ten_max);
+        bool clear = f_surely_elastic(st, s0f, anphi, amc, ten_max);
+        if (!clear) {
+            float p[3];
+            f_principal_values(st, 0.f, p);
+            clear = f_clearly_elastic(p, s0f, anphi, amc, ten_max);
         }
-        float amc, anphi, anpsi, hardn, ten_max;
-        // the elastic tests exactly as the pass without a closure applies them
-        const float plsf = (float)pls, s0f = (float)s0;
-        f_plastic_props(F, xf, plsf, amc, anphi, ten_max);
-        elastic(xf.bulkm, xf.shearm, de, s);
-        float p[3];
-        if (!f_surely_elastic(s, s0f, anphi, amc, ten_max) &&
-            (f_principal_values(s, 0.f, p), !f_clearly_elastic(p, s0f, anphi, amc, ten_max))) {
-            kind = 2;
+        if (clear) {
+            float s[6];
+            bool plastic = true;
+            if (RHEOL == 7) {
+                const float visc = f_visc(F, xf, f_elem_T(d, c), edot);
+                const float dv = (float)(d.vol[e] / d.vol_old[e] - 1);
+                float sv[6];
+                for (int i = 0; i < 6; ++i) sv[i] = so[i];
+                maxwell(xf.bulkm, xf.shearm, visc, dt, dv, de, sv);
+                if (f_viscous_wins(xf, so, de, sv, st, 0.0, dt, visc)) {
+                    plastic = false;
+                    for (int i = 0; i < 6; ++i) s[i] = sv[i];
+                }
+            }
+            if (plastic) {
+                for (int i = 0; i < 6; ++i) s[i] = st[i];
+                d.dpls[e] = 0.f;
+            }
+            const float dpv = tr3(s) - tr3(so);
+            f_store6(d.stress, E, e, s);
+            d.dp[e] = dpv;
+            d.tmp_sg[e] = dpv * d.c_vol[e];
+        } else {
+            pending = true;
+        }
+    }
+    list_append(&d.clk->npend, d.pend, pending, e);
+}
+
+constexpr int kNnListBlock = 128;
+
+struct NnListSmem {
+    __nv_bfloat16 w1[kMlpHid * kMlpIn], w2[kMlpHid * kMlpHid], w3[kMlpOut * kMlpHid];
+    float b1[kMlpHid], b2[kMlpHid], b3[kMlpOut];
+    __nv_bfloat16 x[kNnListBlock / 32][32 * kMlpIn];       // two 16-row tiles per warp
+    __nv_bfloat16 h1[kNnListBlock / 32][16 * kHStride], h2[kNnListBlock / 32][16 * kHStride];
+    float y[kNnListBlock / 32][32 * kMlpOut];
+};
+
+// E-B2
+template <int RHEOL>
+__global__ void __launch_bounds__(kNnListBlock) kf_nn_list(DevF d, const MlpDev *__restrict__ net)
+{
+    const unsigned npend = d.clk->npend;
+    if (npend == 0) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    NnListSmem &S = *reinterpret_cast<NnListSmem *>(smem_raw);
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    {
+        const uint4 *src = reinterpret_cast<const uint4 *>(net->w1);
+        uint4 *dst = reinterpret_cast<uint4 *>(S.w1);
+        constexpr int nvec = (int)(sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3)) / 16;
+        for (int i = tid; i < nvec; i += kNnListBlock) dst[i] = __ldg(src + i);
+        for (int i = tid; i < kMlpHid; i += kNnListBlock) {
+            S.b1[i] = net->b1[i];
+            S.b2[i] = net->b2[i];
+        }
+        if (tid < kMlpOut) S.b3[tid] = net->b3[tid];
+    }
+    __syncthreads();
+    const ConstsF &F = *d.F;
+    const float tol = net->tol;
+    float pls_sat = 0.f;       // past the largest pls1 the plastic properties no longer change
+    for (int m = 0; m < F.nmat; ++m) pls_sat = fmaxf(pls_sat, F.pls1[m]);
+    unsigned long long ncand = 0, naccept = 0;
+    const unsigned nwarp = gridDim.x * (kNnListBlock / 32);
+    for (unsigned base = (blockIdx.x * (kNnListBlock / 32) + w) * 32u; base < npend; base += nwarp * 32u) {
+        const unsigned j = base + lane;
+        const bool valid = j < npend;
+        const int e = valid ? d.pend[j] : 0;
+        FTrial q;
+        NnCand cd = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float raw[kMlpIn];
+        bool cand = false;
+        if (valid) {
+            f_trial_from_state<RHEOL>(d, e, q);
+            const MixF &xf = F.mix[q.mix];
+            const float plsf = (float)q.pls, s0f = (float)q.s0;
+            float amc, anphi, anpsi, hardn, ten_max, p[3];
+            f_principal_values(q.s, 0.f, p);
             // FP32 throughout: the tests below have margins of tol S, and the
             // FP32 sums are good to about 1e-7 S
             f_plastic_full(F, xf, plsf, amc, anphi, anpsi, hardn, ten_max);
@@ -218,12 +353,8 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
             const float a1 = xf.bulkm + (4.f / 3.f) * xf.shearm, a2 = xf.bulkm - (2.f / 3.f) * xf.shearm;
             const float den = a1 - a2 * anpsi + a1 * anphi * anpsi - a2 * anphi + 2.f * sqrtf(anphi) * hardn;
             cd.alam = fs / den;
-            // past the largest pls1 the plastic properties no longer change,
-            // so the network sees the plastic strain saturated there
-            float pls_sat = 0.f;
-            for (int m = 0; m < F.nmat; ++m) pls_sat = fmaxf(pls_sat, F.pls1[m]);
             float nb[6], qb[6], lam[3];
-            if (fs < -tol * cd.S && h < -tol * cd.S && nn_basis(s, p, nb, qb, lam)) {
+            if (fs < -tol * cd.S && h < -tol * cd.S && nn_basis(q.s, p, nb, qb, lam)) {
                 raw[0] = lam[0];
                 raw[1] = lam[1];
                 raw[2] = lam[2];
@@ -235,7 +366,7 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                     inside = inside && raw[i] >= net->env_lo[i] && raw[i] <= net->env_hi[i];
                 }
                 if (inside) {
-                    kind = 1;
+                    cand = true;
                     // each input enters as a BF16 pair, x = hi + lo / 256, so that
                     // the network sees it to about 16 significant bits
                     for (int i = 3; i >= 0; --i) {
@@ -246,153 +377,93 @@ __global__ void __launch_bounds__(kNnBlock) kf_fe_b_nn(DevF d, const MlpDev *__r
                     }
                 }
             }
-            for (int i = 0; i < 6; ++i) {
-                S.so[i][tid] = so[i];
-                S.de[i][tid] = de[i];
-            }
         }
-    }
-
-    float sp[6];
-    double depls = 0.0;
-    // CTAs whose elements are all elastic skip the network and the queue
-    if (__syncthreads_or(kind != 0)) {
-        // ---- compaction of the network candidates ------------------------
-        const unsigned cmask = __ballot_sync(0xffffffffu, kind == 1);
-        if (lane == 0) S.wcount[w] = __popc(cmask);
-        __syncthreads();
-        int nc = 0, slot = 0;
-        for (int i = 0; i < kNnBlock / 32; ++i) {
-            if (i == w) slot = nc + __popc(cmask & ((1u << lane) - 1u));
-            nc += S.wcount[i];
-        }
-        if (kind == 1) {
-            __nv_bfloat16 *xr = S.x + slot * kMlpIn;
-            for (int i = 0; i < kMlpIn; i += 2)
-                *reinterpret_cast<uint32_t *>(xr + i) = pack_bf16(i < kMlpInUsed ? raw[i] : 0.f,
-                                                                  i + 1 < kMlpInUsed ? raw[i + 1] : 0.f);
-        }
+        // the candidates of this warp, packed into one or two 16-row tiles
+        const unsigned cm = __ballot_sync(0xffffffffu, cand);
+        const int nc = __popc(cm), slot = __popc(cm & ((1u << lane) - 1u));
         const int ntile = (nc + 15) >> 4;
-        if (tid >= nc && tid < ntile * 16)      // zero rows that pad the last tile
-            for (int i = 0; i < kMlpIn; i += 2) *reinterpret_cast<uint32_t *>(S.x + tid * kMlpIn + i) = 0u;
-        if (nc > 0) {
-            // the network's parameters, once per CTA that has candidates
-            const uint4 *src = reinterpret_cast<const uint4 *>(net->w1);
-            uint4 *dst = reinterpret_cast<uint4 *>(S.w1);
-            constexpr int nvec = (int)(sizeof(S.w1) + sizeof(S.w2) + sizeof(S.w3)) / 16;
-            for (int i = tid; i < nvec; i += kNnBlock) dst[i] = __ldg(src + i);
-            for (int i = tid; i < kMlpHid; i += kNnBlock) {
-                S.b1[i] = net->b1[i];
-                S.b2[i] = net->b2[i];
-            }
-            if (tid < kMlpOut) S.b3[tid] = net->b3[tid];
-        }
-        __syncthreads();
-        for (int t = w; t < ntile; t += kNnBlock / 32)
-            mlp_forward16(S.x + t * 16 * kMlpIn, S.w1, S.w2, S.w3, S.b1, S.b2, S.b3, S.h1[w], S.h2[w],
-                          S.y + t * 16 * kMlpOut);
-        __syncthreads();
-
-        // ---- judge the predictions ---------------------------------------
-        if (kind == 1) {
+        __nv_bfloat16 *X = S.x[w];
+        if (cand)
+            for (int i = 0; i < kMlpIn; i += 2)
+                *reinterpret_cast<uint32_t *>(X + slot * kMlpIn + i) =
+                    pack_bf16(i < kMlpInUsed ? raw[i] : 0.f, i + 1 < kMlpInUsed ? raw[i + 1] : 0.f);
+        if (lane >= nc && lane < ntile * 16)      // rows that pad the last tile
+            for (int i = 0; i < kMlpIn; i += 2) *reinterpret_cast<uint32_t *>(X + lane * kMlpIn + i) = 0u;
+        __syncwarp();
+        for (int t = 0; t < ntile; ++t)
+            mlp_forward16(X + t * 16 * kMlpIn, S.w1, S.w2, S.w3, S.b1, S.b2, S.b3, S.h1[w], S.h2[w],
+                          S.y[w] + t * 16 * kMlpOut);
+        __syncwarp();
+        bool accepted = false;
+        if (cand) {
             // R = a I + (b / D) n + (c / D) dev(n n), the return per unit
             // multiplier; sigma = trial - 2 G alam R
-            const MixF &xf = F.mix[mixid];
-            const float *yo = S.y + slot * kMlpOut;
-            float nb[6], qb[6], lam[3], p[3];
-            f_principal_values(s, 0.f, p);
-            nn_basis(s, p, nb, qb, lam);
+            const MixF &xf = F.mix[q.mix];
+            const float *yo = S.y[w] + slot * kMlpOut;
+            float nb[6], qb[6], lam[3], p[3], sp[6];
+            f_principal_values(q.s, 0.f, p);
+            nn_basis(q.s, p, nb, qb, lam);
             const float D = nn_pole(lam);
             const float a = yo[0] * net->out_scale[0];
             const float b = yo[1] * net->out_scale[1] / D, c = yo[2] * net->out_scale[2] / D;
             const float g2 = 2.f * xf.shearm * cd.alam;
-            for (int i = 0; i < 6; ++i) sp[i] = s[i] - g2 * ((i < 3 ? a : 0.f) + b * nb[i] + c * qb[i]);
-            const float dp = fabsf(cd.alam) * yo[3] * net->out_scale[3];
+            for (int i = 0; i < 6; ++i) sp[i] = q.s[i] - g2 * ((i < 3 ? a : 0.f) + b * nb[i] + c * qb[i]);
+            const float dpl = fabsf(cd.alam) * yo[3] * net->out_scale[3];
             f_principal_values(sp, 0.f, p);
             const float r = p[0] - cd.anphi * p[2] + cd.cf - 2.f * sqrtf(cd.anphi) * cd.hardn * cd.alam;
-            bool ok = fabsf(D) > 1e-4f && dp > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
+            bool ok = fabsf(D) > 1e-4f && dpl > 0.f && fabsf(r) <= tol * cd.S && p[2] + cd.ft_shift < 0.f;
             for (int i = 0; i < 6; ++i) ok = ok && isfinite(sp[i]);
             if (RHEOL == 7 && ok) {
                 // the Maxwell/plastic choice of rheology.cxx:628-638 must be clear
-                const float jv = second_invariant2(sv), jp = second_invariant2(sp);
+                const float jv = second_invariant2(q.sv), jp = second_invariant2(sp);
                 ok = fabsf(jv - jp) > tol * fmaxf(jv, jp);
             }
-            if (ok)
-                depls = dp;
-            else
-                kind = 2;
-        }
-        const unsigned amask = __ballot_sync(0xffffffffu, kind == 1);
-        const unsigned xmask = __ballot_sync(0xffffffffu, kind == 2);
-        if (lane == 0) {
-            if (cmask) atomicAdd(&d.clk->nn_cand, (unsigned long long)__popc(cmask));
-            if (amask) atomicAdd(&d.clk->nn_accept, (unsigned long long)__popc(amask));
-            if (xmask) atomicAdd(&d.clk->fp64_returns, (unsigned long long)__popc(xmask));
-        }
-
-        // ---- exact FP64 return map for the compacted rest -----------------
-        __syncthreads();     // every warp has read its wcount entry above
-        if (lane == 0) S.wcount[w] = __popc(xmask);
-        __syncthreads();
-        int nx = 0, xslot = 0;
-        for (int i = 0; i < kNnBlock / 32; ++i) {
-            if (i == w) xslot = nx + __popc(xmask & ((1u << lane) - 1u));
-            nx += S.wcount[i];
-        }
-        if (kind == 2) S.queue[xslot] = tid;
-        __syncthreads();
-        int flags = 0;
-        if (tid < nx) {
-            const int j = S.queue[tid];
-            const int ej = blockIdx.x * kNnBlock + j;
-            float sj[6], dej[6], out[6];
-            for (int i = 0; i < 6; ++i) {
-                sj[i] = S.so[i][j];
-                dej[i] = S.de[i][j];
+            if (ok) {
+                accepted = true;
+                f_finish<RHEOL>(d, e, q, sp, dpl, true);
             }
-            const Consts &K = *d.K;
-            double dpj;
-            flags = ep_fp64(K, K.M.mix[d.mix[ej]], d.pls[ej], d.s0[ej], sj, dej, out, dpj);
-            for (int i = 0; i < 6; ++i) S.res[i][j] = out[i];
-            S.resd[j] = dpj;
         }
-        __syncthreads();
-        unsigned solved = __ballot_sync(0xffffffffu, flags & 1), ql = __ballot_sync(0xffffffffu, flags & 2);
-        if (lane == 0) {
-            if (solved) atomicAdd(&d.clk->eig, (unsigned long long)__popc(solved));
-            if (ql) atomicAdd(&d.clk->ql, (unsigned long long)__popc(ql));
-        }
+        ncand += nc;
+        naccept += __popc(__ballot_sync(0xffffffffu, accepted));
+        list_append(&d.clk->nexact, d.exact, valid && !accepted, e);
+        __syncwarp();      // the tile buffers are reused by the next round
     }
-    if (!live) return;
+    if (lane == 0) {
+        if (ncand) atomicAdd(&d.clk->nn_cand, ncand);
+        if (naccept) atomicAdd(&d.clk->nn_accept, naccept);
+    }
+}
 
-    // ---- results -------------------------------------------------------------
-    if (kind == 2) {
-        for (int i = 0; i < 6; ++i) sp[i] = S.res[i][tid];
-        depls = S.resd[tid];
-    } else if (kind == 0) {
-        for (int i = 0; i < 6; ++i) sp[i] = s[i];
-        depls = 0.0;
+// E-B3: the exact FP64 return map over a list
+template <int RHEOL>
+__global__ void kf_exact_list(DevF d, int from_pending)
+{
+    const unsigned n = from_pending ? d.clk->npend : d.clk->nexact;
+    const int *list = from_pending ? d.pend : d.exact;
+    unsigned nsolved = 0, nql = 0, nret = 0;
+    for (unsigned j = gtid(); j < n; j += gridDim.x * blockDim.x) {
+        const int e = list[j];
+        FTrial q;
+        f_trial_from_state<RHEOL>(d, e, q);
+        const Consts &K = *d.K;
+        float sp[6];
+        double depls;
+        const int flags = ep_fp64(K, K.M.mix[q.mix], q.pls, q.s0, q.so, q.de, sp, depls);
+        f_finish<RHEOL>(d, e, q, sp, depls, false);
+        nsolved += (flags & 1) ? 1u : 0u;
+        nql += (flags & 2) ? 1u : 0u;
+        ++nret;
     }
-    bool plastic = true;
-    if (RHEOL == 7) {
-        if (kind == 1)
-            plastic = second_invariant2(sv) >= second_invariant2(sp);
-        else
-            plastic = !f_viscous_wins(F.mix[mixid], so, de, sv, sp, depls, dt, visc);
+    for (int o = 16; o > 0; o >>= 1) {
+        nsolved += __shfl_down_sync(0xffffffffu, nsolved, o);
+        nql += __shfl_down_sync(0xffffffffu, nql, o);
+        nret += __shfl_down_sync(0xffffffffu, nret, o);
     }
-    if (plastic) {
-        for (int i = 0; i < 6; ++i) s[i] = sp[i];
-        pls += depls;
-        dpls = (float)depls;
-    } else {
-        for (int i = 0; i < 6; ++i) s[i] = sv[i];
+    if ((threadIdx.x & 31) == 0) {
+        if (nsolved) atomicAdd(&d.clk->eig, (unsigned long long)nsolved);
+        if (nql) atomicAdd(&d.clk->ql, (unsigned long long)nql);
+        if (nret) atomicAdd(&d.clk->fp64_returns, (unsigned long long)nret);
     }
-    float dpv = tr3(s) - tr3(so);
-    f_store6(d.stress, E, e, s);
-    d.pls[e] = pls;
-    d.dpls[e] = dpls;
-    d.dp[e] = dpv;
-    d.tmp_sg[e] = dpv * d.c_vol[e];
 }
 
 }  // namespace des

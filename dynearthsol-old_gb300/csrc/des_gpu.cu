@@ -28,6 +28,7 @@ inline int blocks(long long n, int b) { return (int)((n + b - 1) / b); }
 
 struct des_gpu {
     int device = 0;
+    int sms = 1;                          // multiprocessors of the device
     cudaStream_t stream = nullptr;
     int nnode = 0, nelem = 0, nmat = 0;
     des_params P;
@@ -508,12 +509,22 @@ void launch_pass(des_gpu *g, int k)
         switch (k) {
         case 0: kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f); break;
         case 1:
-            if (g->closure && g->hF.rheol == 7)
-                kf_fe_b_nn<7><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
-            else if (g->closure)
-                kf_fe_b_nn<5><<<eb, kNnBlock, sizeof(NnSmem), st>>>(f, g->dnet);
-            else
+            if (g->hF.rheol == 5 || g->hF.rheol == 7) {
+                // elastic elements, then the network (with a closure), then
+                // the exact return map, each over a dense list
+                const int nn_grid = 4 * g->sms, exact_grid = 8 * g->sms;
+                if (g->hF.rheol == 7) {
+                    kf_fe_b_ep<7><<<eb, kElemBlock, 0, st>>>(f);
+                    if (g->closure) kf_nn_list<7><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
+                    kf_exact_list<7><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
+                } else {
+                    kf_fe_b_ep<5><<<eb, kElemBlock, 0, st>>>(f);
+                    if (g->closure) kf_nn_list<5><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
+                    kf_exact_list<5><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
+                }
+            } else {
                 kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
+            }
             break;
         case 2: kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f); break;
         case 3: kf_fe_c<<<eb, kElemBlock, 0, st>>>(f); break;
@@ -691,6 +702,8 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
         return DES_ERR_CUDA;
     }
     cudaGetDevice(&g->device);
+    cudaDeviceGetAttribute(&g->sms, cudaDevAttrMultiProcessorCount, g->device);
+    if (g->sms < 1) g->sms = 1;
     g->P = *p;
     g->nnode = m->nnode;
     g->nelem = m->nelem;
@@ -768,6 +781,7 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
             (rc = dev_alloc(g, &f.c_vol, E)) || (rc = dev_alloc(g, &f.c_mass, E)) ||
             (rc = dev_alloc(g, &f.c_tmass, E)) || (rc = dev_alloc(g, &f.c_trdv, E)) ||
             (rc = dev_alloc(g, &f.s0, E)) || (rc = dev_alloc(g, &f.f0, 12 * E)) ||
+            (rc = dev_alloc(g, &f.pend, E)) || (rc = dev_alloc(g, &f.exact, E)) ||
             (rc = dev_alloc(g, &g->dF, 1)))
             return fail(rc);
         f.nnode = d.nnode;
@@ -921,7 +935,10 @@ long long des_gpu_device_bytes(const des_gpu *g) { return g ? g->bytes : 0; }
 int des_gpu_kernels_per_step(const des_gpu *g)
 {
     if (!g) return 0;
-    return kStepKernels + ((g->hK.stress_bc_sides && g->d.sbc.nbf > 0) ? 1 : 0);
+    int n = kStepKernels + ((g->hK.stress_bc_sides && g->d.sbc.nbf > 0) ? 1 : 0);
+    // the FP32 form's elasto-plastic stress pass: the exact list, the network
+    if (g->prec == DES_PREC_FP32 && (g->hF.rheol == 5 || g->hF.rheol == 7)) n += g->closure ? 2 : 1;
+    return n + (g->avg_interval > 0 ? 1 : 0);
 }
 
 int des_gpu_upload(des_gpu *g, const des_state_view *h, unsigned mask)
@@ -1462,10 +1479,6 @@ int des_gpu_set_closure(des_gpu *g, const des_mlp *net)
     }
     DES_CUDA(cudaMemcpyAsync(g->dnet, &h, sizeof(h), cudaMemcpyHostToDevice, g->stream));
     DES_CUDA(cudaStreamSynchronize(g->stream));
-    DES_CUDA(cudaFuncSetAttribute(kf_fe_b_nn<5>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(NnSmem)));
-    DES_CUDA(cudaFuncSetAttribute(kf_fe_b_nn<7>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)sizeof(NnSmem)));
     g->closure = true;
     return DES_OK;
 }

@@ -43,6 +43,7 @@ struct Clock {
     unsigned long long ql, eig;
     unsigned long long nlog;                    // return-map records seen (logging launches)
     unsigned long long nn_cand, nn_accept, fp64_returns;   // learned-closure counters
+    unsigned npend, nexact;          // list lengths of the FP32 form's stress pass
 };
 
 // The boundary facets of apply_stress_bcs (bc.cxx:503-595) and, for every

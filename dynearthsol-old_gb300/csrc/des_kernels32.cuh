@@ -72,6 +72,7 @@ struct DevF {
     const ConstsF *F;
     Clock *clk;
     StressBc sbc;
+    int *pend, *exact;                              // [E] element lists of the stress pass
 };
 
 __device__ __forceinline__ void f_load_vel4(const DevF &d, int4 c, float V[4][3])
@@ -406,6 +407,8 @@ __global__ void kf_fn_a(DevF d)
     if (n == 0) {
         d.clk->steps += 1;
         d.clk->time += dt;
+        d.clk->npend = 0;
+        d.clk->nexact = 0;
     }
     if (n >= d.nnode) return;
     const size_t E = d.nelem;
