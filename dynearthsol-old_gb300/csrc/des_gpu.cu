@@ -124,7 +124,9 @@ int check_params(const des_params &p, int nmat)
 {
     if (p.nmat != nmat || nmat < 1 || nmat > DES_MAX_MAT) return DES_ERR_ARG;
     if (p.is_plane_strain) return DES_ERR_UNSUPPORTED;
-    if (p.surface_process_option != 0) return DES_ERR_UNSUPPORTED;
+    // bc.cxx:765-777: 0 none, 1 diffusion, 101 the custom template
+    if (p.surface_process_option != 0 && p.surface_process_option != 1 && p.surface_process_option != 101)
+        return DES_ERR_OPTION;
     if (p.rheol_type != DES_RH_ELASTIC && p.rheol_type != DES_RH_VISCOUS &&
         p.rheol_type != DES_RH_MAXWELL && p.rheol_type != DES_RH_EP && p.rheol_type != DES_RH_EVP)
         return DES_ERR_OPTION;
@@ -312,6 +314,8 @@ int build_consts(des_gpu *g)
     K.elastic_foundation = (p.gravity != 0 && p.has_elastic_foundation) ? 1 : 0;
     K.elastic_foundation_constant = p.elastic_foundation_constant;
     K.winkler_delta_rho = p.winkler_delta_rho;
+    K.surface_process_option = p.surface_process_option;
+    K.surface_diffusivity = p.surface_diffusivity;
     g->stress_bcs = K.stress_bc_sides != 0 || K.elastic_foundation;
     if (cudaMemcpyAsync(g->dK, &g->hK, sizeof(Consts), cudaMemcpyHostToDevice, g->stream) !=
         cudaSuccess)
@@ -499,6 +503,16 @@ int prime(des_gpu *g)
     return DES_OK;
 }
 
+// surface_processes (bc.cxx:760-782), after update_coordinate
+void launch_surface(des_gpu *g)
+{
+    const int opt = g->P.surface_process_option;
+    if (opt == 0) return;
+    if (opt == 1 && g->d.bf.nbf > 0)
+        k_surface_facets<<<blocks(g->d.bf.nbf, 128), 128, 0, g->stream>>>(g->d);
+    k_surface_nodes<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
+}
+
 // pass k of N-A, E-B, N-B, E-C, N-C (0..4) of one step
 void launch_pass(des_gpu *g, int k)
 {
@@ -529,9 +543,10 @@ void launch_pass(des_gpu *g, int k)
         case 2: kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f); break;
         case 3: kf_fe_c<<<eb, kElemBlock, 0, st>>>(f); break;
         default:
-            if (g->hK.stress_bc_sides && g->d.sbc.nbf > 0)
-                k_stress_bc_facets<<<blocks(g->d.sbc.nbf, 128), 128, 0, st>>>(g->d);
+            if (g->hK.stress_bc_sides && g->d.bf.nbf > 0)
+                k_stress_bc_facets<<<blocks(g->d.bf.nbf, 128), 128, 0, st>>>(g->d);
             kf_fn_c<<<nb, kNodeBlock, 0, st>>>(f);
+            launch_surface(g);
             break;
         }
     } else {
@@ -547,9 +562,10 @@ void launch_pass(des_gpu *g, int k)
         case 2: k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d); break;
         case 3: k_fe_c<<<eb, kElemBlock, 0, st>>>(d); break;
         default:
-            if (g->hK.stress_bc_sides && d.sbc.nbf > 0)
-                k_stress_bc_facets<<<blocks(d.sbc.nbf, 128), 128, 0, st>>>(d);
+            if (g->hK.stress_bc_sides && d.bf.nbf > 0)
+                k_stress_bc_facets<<<blocks(d.bf.nbf, 128), 128, 0, st>>>(d);
             k_fn_c<<<nb, kNodeBlock, 0, st>>>(d);
+            launch_surface(g);
             break;
         }
     }
@@ -832,9 +848,10 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
         for (int q = 0; q < 3 * nbf; ++q) nf[(size_t)fill[nodes[q]]++] = q / 3;
         int *d_elem, *d_off, *d_nf;
         unsigned char *d_sf;
-        double *d_val;
+        double *d_val, *d_surf;
         if ((rc = dev_alloc(g, &d_elem, (size_t)nbf)) || (rc = dev_alloc(g, &d_sf, (size_t)nbf)) ||
-            (rc = dev_alloc(g, &d_val, 3 * (size_t)nbf)) || (rc = dev_alloc(g, &d_off, N + 1)) ||
+            (rc = dev_alloc(g, &d_val, 3 * (size_t)nbf)) || (rc = dev_alloc(g, &d_surf, 4 * (size_t)nbf)) ||
+            (rc = dev_alloc(g, &d_off, N + 1)) ||
             (rc = dev_alloc(g, &d_nf, (size_t)off[N])))
             return fail(rc);
         if (cudaMemcpy(d_elem, belem.data(), sizeof(int) * nbf, cudaMemcpyHostToDevice) ||
@@ -842,15 +859,16 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
             cudaMemcpy(d_off, off.data(), sizeof(int) * (N + 1), cudaMemcpyHostToDevice) ||
             cudaMemcpy(d_nf, nf.data(), sizeof(int) * nf.size(), cudaMemcpyHostToDevice))
             return fail(DES_ERR_CUDA);
-        StressBc sb;
+        BdryFacets sb;
         sb.nbf = nbf;
         sb.elem = d_elem;
         sb.side_f = d_sf;
         sb.val = d_val;
+        sb.surf = d_surf;
         sb.node_off = d_off;
         sb.node_facet = d_nf;
-        g->d.sbc = sb;
-        g->f.sbc = sb;
+        g->d.bf = sb;
+        g->f.bf = sb;
     }
 
     std::vector<unsigned> ent(4 * E);
@@ -935,7 +953,9 @@ long long des_gpu_device_bytes(const des_gpu *g) { return g ? g->bytes : 0; }
 int des_gpu_kernels_per_step(const des_gpu *g)
 {
     if (!g) return 0;
-    int n = kStepKernels + ((g->hK.stress_bc_sides && g->d.sbc.nbf > 0) ? 1 : 0);
+    int n = kStepKernels + ((g->hK.stress_bc_sides && g->d.bf.nbf > 0) ? 1 : 0);
+    if (g->P.surface_process_option == 1) n += g->d.bf.nbf > 0 ? 2 : 1;
+    if (g->P.surface_process_option == 101) n += 1;
     // the FP32 form's elasto-plastic stress pass: the exact list, the network
     if (g->prec == DES_PREC_FP32 && (g->hF.rheol == 5 || g->hF.rheol == 7)) n += g->closure ? 2 : 1;
     return n + (g->avg_interval > 0 ? 1 : 0);
@@ -1825,8 +1845,8 @@ int des_gpu_update_force(des_gpu *g)
     int rc = begin_fn64(g);
     if (rc) return rc;
     k_force_elem<<<ELEM_GRID(g)>>>(g->d);
-    if (g->hK.stress_bc_sides && g->d.sbc.nbf > 0)
-        k_stress_bc_facets<<<blocks(g->d.sbc.nbf, 128), 128, 0, g->stream>>>(g->d);
+    if (g->hK.stress_bc_sides && g->d.bf.nbf > 0)
+        k_stress_bc_facets<<<blocks(g->d.bf.nbf, 128), 128, 0, g->stream>>>(g->d);
     k_force_node<<<NODE_GRID(g)>>>(g->d, g->hK.is_qs);
     return finish(g);
 }
@@ -1879,6 +1899,7 @@ int des_gpu_update_mesh(des_gpu *g)
     int rc = begin_fn64(g);
     if (rc) return rc;
     k_coord<<<NODE_GRID(g)>>>(g->d);
+    launch_surface(g);
     k_volume<<<ELEM_GRID(g)>>>(g->d, 1);
     k_mass_elem<<<ELEM_GRID(g)>>>(g->d, g->d.T);
     k_mass_node<<<NODE_GRID(g)>>>(g->d);

@@ -28,6 +28,8 @@ struct Consts {
     double winkler_delta_rho, elastic_foundation_constant;
     unsigned stress_bc_sides;   // sides whose facets carry apply_stress_bcs' tractions
     int elastic_foundation;     // the bottom restoring force of apply_stress_bcs
+    int surface_process_option;
+    double surface_diffusivity;
     int damping_option, is_qs, thermal, rheol;
     int vbc_types[10];
     double vbc_values[10];
@@ -46,14 +48,16 @@ struct Clock {
     unsigned npend, nexact;          // list lengths of the FP32 form's stress pass
 };
 
-// The boundary facets of apply_stress_bcs (bc.cxx:503-595) and, for every
-// node, the facets it belongs to in the order the reference subtracts their
-// tractions (side by side, facets in bfacets order).
-struct StressBc {
+// The boundary facets (mesh.cxx:1633-1682, bfacets side by side) and, for
+// every node, the facets it belongs to in that order: the order in which
+// apply_stress_bcs (bc.cxx:503-595) and the surface diffusion (bc.cxx:598-730)
+// accumulate facet terms at a node.
+struct BdryFacets {
     int nbf;
     const int *elem;                // [nbf] element of each facet
     const unsigned char *side_f;    // [nbf] side << 2 | facet of the element
     double *val;                    // [3][nbf] traction p n / 3 on each of its nodes
+    double *surf;                   // [4][nbf] top facets: projected area, slope term of each node
     const int *node_off;            // [nnode + 1]
     const int *node_facet;          // facet indices
 };
@@ -76,7 +80,7 @@ struct Dev {
     Clock *clk;
     float *ret_log;                  // return-map records (logging launches only)
     long long ret_cap;
-    StressBc sbc;
+    BdryFacets bf;
 };
 
 __device__ __forceinline__ int gtid() { return blockIdx.x * blockDim.x + threadIdx.x; }
@@ -627,7 +631,7 @@ __device__ __forceinline__ int facet_node(int f, int j)
 __global__ void k_stress_bc_facets(Dev d)
 {
     const int k = gtid();
-    const StressBc &b = d.sbc;
+    const BdryFacets &b = d.bf;
     if (k >= b.nbf) return;
     const Consts &K = *d.K;
     const int side = b.side_f[k] >> 2, f = b.side_f[k] & 3;
@@ -660,9 +664,68 @@ __global__ void k_stress_bc_facets(Dev d)
     for (int j = 0; j < 3; ++j) b.val[j * b.nbf + k] = p * normal[j] / 3;
 }
 
+// bc.cxx:616-700 (simple_diffusion, 3D) for one facet of the top boundary:
+// its projected area and, for each of its nodes, the FEM slope term that the
+// node's total_slope receives
+__global__ void k_surface_facets(Dev d)
+{
+    const int k = gtid();
+    const BdryFacets &b = d.bf;
+    if (k >= b.nbf || (b.side_f[k] >> 2) != 5) return;
+    const int f = b.side_f[k] & 3;
+    const int4 c4 = d.conn[b.elem[k]];
+    auto pick = [&](int i) { return i == 0 ? c4.x : i == 1 ? c4.y : i == 2 ? c4.z : c4.w; };
+    const int n[3] = {pick(facet_node(f, 0)), pick(facet_node(f, 1)), pick(facet_node(f, 2))};
+    const double X[3] = {d.x[n[0]], d.x[n[1]], d.x[n[2]]};
+    const double Y[3] = {d.y[n[0]], d.y[n[1]], d.y[n[2]]};
+    const double Z[3] = {d.z[n[0]], d.z[n[1]], d.z[n[2]]};
+    const double x01 = X[1] - X[0], y01 = Y[1] - Y[0], x02 = X[2] - X[0], y02 = Y[2] - Y[0];
+    const double projected_area = 0.5 * (x01 * y02 - y01 * x02);
+    const double iv = 1 / (2 * projected_area);
+    const double sx[3] = {iv * (Y[1] - Y[2]), iv * (Y[2] - Y[0]), iv * (Y[0] - Y[1])};
+    const double sy[3] = {iv * (X[2] - X[1]), iv * (X[0] - X[2]), iv * (X[1] - X[0])};
+    b.surf[k] = projected_area;
+    for (int j = 0; j < 3; ++j) {
+        double slope = 0;
+        for (int i = 0; i < 3; ++i) {
+            const double D = sx[j] * sx[i] + sy[j] * sy[i];
+            slope += D * Z[i];
+        }
+        b.surf[(1 + j) * b.nbf + k] = slope * projected_area;
+    }
+}
+
+// bc.cxx:702-712 (option 1) for one node of the top boundary: its totals over
+// its top facets in facet order, then the height change; option 101 (the
+// reference's custom template, bc.cxx:735-757) adds dh = 0
+__global__ void k_surface_nodes(Dev d)
+{
+    const int n = gtid();
+    if (n >= d.nnode || !(d.bcflag[n] & kBoundZ1)) return;
+    const Consts &K = *d.K;
+    if (K.surface_process_option != 1) {
+        d.z[n] += 0.0;
+        return;
+    }
+    const BdryFacets &b = d.bf;
+    double total_dx = 0, total_slope = 0;
+    for (int q = b.node_off[n]; q < b.node_off[n + 1]; ++q) {
+        const int k = b.node_facet[q];
+        if ((b.side_f[k] >> 2) != 5) continue;
+        const int f = b.side_f[k] & 3;
+        const int4 c4 = d.conn[b.elem[k]];
+        auto pick = [&](int i) { return i == 0 ? c4.x : i == 1 ? c4.y : i == 2 ? c4.z : c4.w; };
+        const int j = pick(facet_node(f, 0)) == n ? 0 : pick(facet_node(f, 1)) == n ? 1 : 2;
+        total_dx += b.surf[k];
+        total_slope += b.surf[(1 + j) * b.nbf + k];
+    }
+    const double dh = K.surface_diffusivity * d.clk->dt * total_slope / total_dx;
+    d.z[n] -= dh;
+}
+
 // bc.cxx:568-590 for node n after update_force's gather: the tractions of its
 // boundary facets, then the elastic foundation's restoring force on the bottom
-__device__ __forceinline__ void stress_bc_node(const Consts &K, const StressBc &b, int n, unsigned flag,
+__device__ __forceinline__ void stress_bc_node(const Consts &K, const BdryFacets &b, int n, unsigned flag,
                                                double z, double z0, double f[3])
 {
     if (K.stress_bc_sides && (flag & kBoundAny)) {
@@ -694,7 +757,7 @@ __global__ void k_force_node(Dev d, int damping)
     if (n >= d.nnode) return;
     double f[3];
     force_gather(d, n, f);
-    stress_bc_node(*d.K, d.sbc, n, d.bcflag[n], d.z[n], d.z0[n], f);
+    stress_bc_node(*d.K, d.bf, n, d.bcflag[n], d.z[n], d.z0[n], f);
     if (damping) {
         const Consts &K = *d.K;
         f[0] = damp(K, f[0], d.vx[n]);
@@ -1061,7 +1124,7 @@ __global__ void k_fn_c(Dev d)
     const double dt = d.clk->dt;
     double f[3];
     force_gather(d, n, f);
-    stress_bc_node(K, d.sbc, n, d.bcflag[n], d.z[n], d.z0[n], f);
+    stress_bc_node(K, d.bf, n, d.bcflag[n], d.z[n], d.z0[n], f);
     double v[3] = {d.vx[n], d.vy[n], d.vz[n]};
     if (K.is_qs) {
         f[0] = damp(K, f[0], v[0]);

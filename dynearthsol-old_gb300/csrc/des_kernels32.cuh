@@ -71,7 +71,7 @@ struct DevF {
     const Consts *K;
     const ConstsF *F;
     Clock *clk;
-    StressBc sbc;
+    BdryFacets bf;
     int *pend, *exact;                              // [E] element lists of the stress pass
 };
 
@@ -597,7 +597,7 @@ __global__ void kf_fn_c(DevF d)
         h[2] -= d.f0[(i + 8) * E + e];
     }
     // the boundary tractions balance the FP64 reference part: FP64 as well
-    stress_bc_node(K, d.sbc, n, d.bcflag[n], d.z[n], d.z0[n], h);
+    stress_bc_node(K, d.bf, n, d.bcflag[n], d.z[n], d.z0[n], h);
     float f[3] = {(float)(h[0] + (double)g[0]), (float)(h[1] + (double)g[1]),
                   (float)(h[2] + (double)g[2])};
     float v[3] = {d.vx[n], d.vy[n], d.vz[n]};

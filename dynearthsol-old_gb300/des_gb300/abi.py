@@ -71,7 +71,7 @@ class Params(C.Structure):
     _fields_ = [
         ("gravity", C.c_double), ("inertial_scaling", C.c_double), ("dt_fraction", C.c_double),
         ("fixed_dt", C.c_double), ("damping_factor", C.c_double),
-        ("damping_option", C.c_int), ("ref_pressure_option", C.c_int),
+        ("surface_diffusivity", C.c_double), ("damping_option", C.c_int), ("ref_pressure_option", C.c_int),
         ("surface_process_option", C.c_int), ("is_quasi_static", C.c_int),
         ("has_thermal_diffusion", C.c_int),
         ("surface_temperature", C.c_double), ("winkler_delta_rho", C.c_double),

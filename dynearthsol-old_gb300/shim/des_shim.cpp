@@ -26,6 +26,7 @@ des_params make_params(const Param &p, const Variables &var)
     q.dt_fraction = p.control.dt_fraction;
     q.fixed_dt = p.control.fixed_dt;
     q.damping_factor = p.control.damping_factor;
+    q.surface_diffusivity = p.control.surface_diffusivity;
     q.damping_option = p.control.damping_option;
     q.ref_pressure_option = p.control.ref_pressure_option;
     q.surface_process_option = p.control.surface_process_option;

@@ -33,7 +33,7 @@ extern "C" {
 #define DES_ERR_ARG         2   /* bad pointer, size or mask */
 #define DES_ERR_CUDA        3   /* a CUDA runtime call failed */
 #define DES_ERR_NOMEM       4   /* device allocation failed */
-#define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / surface processes / fp32 closure not built */
+#define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / PREM reference pressure / closure preconditions */
 #define DES_ERR_SIZE        6   /* size above a fixed limit of the entry point */
 #define DES_ERR_DT         11   /* dt <= 0 (geometry.cxx:321-325) or NaN/Inf coordinates (output.cxx:195-208) */
 #define DES_ERR_TOPOLOGY   12   /* a segment is on no element (mesh.cxx:1676-1678) */
@@ -100,6 +100,7 @@ typedef struct des_params {
     double dt_fraction;
     double fixed_dt;
     double damping_factor;
+    double surface_diffusivity;   /* surface_process_option 1 (bc.cxx:598-730) */
     int    damping_option;
     int    ref_pressure_option;
     int    surface_process_option;

@@ -1157,11 +1157,60 @@ int dso_compute_shape_fn(dso *o, des_state_view *st)
     return DES_OK;
 }
 
-// dynearthsol.cxx:237-261 (surface_processes option 0 is a no-op)
+namespace {
+// bc.cxx:598-730 (simple_diffusion, 3D): the heights of the top surface
+// diffuse; every top facet adds its horizontal projected area to its nodes'
+// total_dx and its FEM slope term to their total_slope, in bfacets order
+void surface_diffusion(dso *o, des_state_view *st)
+{
+    double *x = st->coord;
+    std::vector<double> total_dx(o->nnode, 0.0), total_slope(o->nnode, 0.0);
+    for (const auto &fc : o->bfacets[5]) {
+        const int *c = &o->conn[4 * (size_t)fc.first];
+        const int n[3] = {c[kFacet[fc.second][0]], c[kFacet[fc.second][1]], c[kFacet[fc.second][2]]};
+        auto X = [&](int i, int d) { return x[3 * (size_t)n[i] + d]; };
+        const double x01 = X(1, 0) - X(0, 0), y01 = X(1, 1) - X(0, 1);
+        const double x02 = X(2, 0) - X(0, 0), y02 = X(2, 1) - X(0, 1);
+        const double projected_area = 0.5 * (x01 * y02 - y01 * x02);
+        for (int i = 0; i < 3; ++i) total_dx[n[i]] += projected_area;
+        const double iv = 1 / (2 * projected_area);
+        const double sx[3] = {iv * (X(1, 1) - X(2, 1)), iv * (X(2, 1) - X(0, 1)), iv * (X(0, 1) - X(1, 1))};
+        const double sy[3] = {iv * (X(2, 0) - X(1, 0)), iv * (X(0, 0) - X(2, 0)), iv * (X(1, 0) - X(0, 0))};
+        for (int j = 0; j < 3; ++j) {
+            double slope = 0;
+            for (int k = 0; k < 3; ++k) {
+                const double D = sx[j] * sx[k] + sy[j] * sy[k];
+                slope += D * X(k, 2);
+            }
+            total_slope[n[j]] += slope * projected_area;
+        }
+    }
+    for (int nd : o->bnodes[5]) {
+        const double dh = o->P.surface_diffusivity * st->dt * total_slope[nd] / total_dx[nd];
+        x[3 * (size_t)nd + 2] -= dh;
+    }
+}
+
+// bc.cxx:760-782: option 1 diffuses the surface; option 101 is the
+// reference's template for a custom rule, which adds dh = 0 to each top node
+int surface_processes(dso *o, des_state_view *st)
+{
+    switch (o->P.surface_process_option) {
+    case 0: return DES_OK;
+    case 1: surface_diffusion(o, st); return DES_OK;
+    case 101:
+        for (int nd : o->bnodes[5]) st->coord[3 * (size_t)nd + 2] += 0.0;
+        return DES_OK;
+    default: return DES_ERR_OPTION;
+    }
+}
+}  // namespace
+
+// dynearthsol.cxx:237-261
 int dso_update_mesh(dso *o, des_state_view *st)
 {
-    if (o->P.surface_process_option != 0) return DES_ERR_UNSUPPORTED;
     dso_update_coordinate(o, st);
+    if (int rc = surface_processes(o, st)) return rc;
     // the reference swaps the two vectors (dynearthsol.cxx:248); the caller's
     // buffers stay in place here, so copy instead
     std::memcpy(st->volume_old, st->volume, sizeof(double) * o->nelem);
@@ -1272,7 +1321,6 @@ int dso_init_fields(dso *o, des_state_view *st)
 int dso_step(dso *o, des_state_view *st, int nsteps)
 {
     const des_params &P = o->P;
-    if (P.surface_process_option != 0) return DES_ERR_UNSUPPORTED;
     for (int it = 0; it < nsteps; ++it) {
         st->steps++;
         st->time += st->dt;
@@ -1287,7 +1335,7 @@ int dso_step(dso *o, des_state_view *st, int nsteps)
         if (rc) return rc;
         dso_update_velocity(o, st);
         dso_apply_vbcs(o, st);
-        dso_update_mesh(o, st);
+        if (int rc = dso_update_mesh(o, st)) return rc;
         if (P.rheol_type & DES_RH_ELASTIC) dso_rotate_stress(o, st);
         if (st->steps % 10 == 0) {
             double dt;

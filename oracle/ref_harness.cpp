@@ -54,7 +54,7 @@ void fill_param(Param &p, const des_params &q, int nmat)
     p.control.damping_option = q.damping_option;
     p.control.ref_pressure_option = q.ref_pressure_option;
     p.control.surface_process_option = q.surface_process_option;
-    p.control.surface_diffusivity = 0;
+    p.control.surface_diffusivity = q.surface_diffusivity;
     p.control.is_quasi_static = q.is_quasi_static != 0;
     p.control.has_thermal_diffusion = q.has_thermal_diffusion != 0;
     p.control.has_hydration_processes = false;
@@ -376,8 +376,9 @@ int dsr_update_mesh(dsr *h)
 {
     Param &param = h->param;
     Variables &var = h->var;
-    // dynearthsol.cxx:237-261 (surface_processes option 0 does nothing)
+    // dynearthsol.cxx:237-261
     update_coordinate(var, *var.coord);
+    surface_processes(param, var, *var.coord);
     var.volume->swap(*var.volume_old);
     compute_volume(*var.coord, *var.connectivity, *var.volume);
     compute_mass(param, var, *var.connectivity, *var.volume, *var.mat, var.max_vbc_val, *var.volume_n,

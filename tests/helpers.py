@@ -94,6 +94,10 @@ OPTION_VARIANTS = {
                             mats=dict(cohesion0=[1e9], cohesion1=[1e9]),
                             vbc=([1, 1, 1, 1, 2, 0, 0, 0, 0, 0],
                                  [-0.01 / _YR, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    # surface processes inside update_mesh (bc.cxx:760-782): diffusion of the
+    # top surface, and the custom-rule template
+    "surface": _variant("surface", params=dict(surface_process_option=1, surface_diffusivity=1.0)),
+    "surface_custom": _variant("surface_custom", params=dict(surface_process_option=101)),
     "mats16": _variant("mats16", nz=6, nlayers=16,
                        layer_rho0=tuple(2700.0 + 40.0 * k for k in range(16)),
                        layer_depths=tuple((k + 1) / 16 for k in range(15)),
