@@ -131,7 +131,7 @@ int check_params(const des_params &p, int nmat)
         p.rheol_type != DES_RH_MAXWELL && p.rheol_type != DES_RH_EP && p.rheol_type != DES_RH_EVP)
         return DES_ERR_OPTION;
     if (p.damping_option < 0 || p.damping_option > 4) return DES_ERR_OPTION;
-    if (p.ref_pressure_option != 0 && p.gravity != 0) return DES_ERR_UNSUPPORTED;
+    if (p.ref_pressure_option < 0 || p.ref_pressure_option > 2) return DES_ERR_OPTION;
     if (p.precision != DES_PREC_FP64 && p.precision != DES_PREC_FP32) return DES_ERR_UNSUPPORTED;
     const des_matvec *vs[] = {&p.rho0, &p.alpha, &p.bulk_modulus, &p.shear_modulus,
                               &p.visc_exponent, &p.visc_coefficient, &p.visc_activation_energy,
@@ -315,6 +315,7 @@ int build_consts(des_gpu *g)
     K.elastic_foundation_constant = p.elastic_foundation_constant;
     K.winkler_delta_rho = p.winkler_delta_rho;
     K.surface_process_option = p.surface_process_option;
+    K.ref_pressure_option = p.ref_pressure_option;
     K.surface_diffusivity = p.surface_diffusivity;
     g->stress_bcs = K.stress_bc_sides != 0 || K.elastic_foundation;
     if (cudaMemcpyAsync(g->dK, &g->hK, sizeof(Consts), cudaMemcpyHostToDevice, g->stream) !=
@@ -1957,7 +1958,9 @@ int des_gpu_init_fields(des_gpu *g)
     if (g->prec == DES_PREC_FP32) {
         int rc = init_fields_fp32(g);
         if (rc) return rc;
-        g->P.compensation_pressure = g->P.gravity != 0 ? g->P.rho0.v[0] * g->P.gravity * g->P.zlength : 0;
+        g->P.compensation_pressure =
+            g->P.gravity != 0 ? ref_pressure(g->P.ref_pressure_option, g->P.rho0.v[0], g->P.gravity, -g->P.zlength)
+                              : 0;
         g->hK.compensation_pressure = g->P.compensation_pressure;
         DES_CUDA(cudaMemcpyAsync(&g->dK->compensation_pressure, &g->hK.compensation_pressure,
                                  sizeof(double), cudaMemcpyHostToDevice, g->stream));
@@ -1984,7 +1987,8 @@ int des_gpu_init_fields(des_gpu *g)
     k_vbcs<<<NODE_GRID(g)>>>(d);
     if (g->P.gravity != 0) {
         k_init_stress<<<ELEM_GRID(g)>>>(d);
-        g->P.compensation_pressure = g->P.rho0.v[0] * g->P.gravity * g->P.zlength;
+        g->P.compensation_pressure =
+            ref_pressure(g->P.ref_pressure_option, g->P.rho0.v[0], g->P.gravity, -g->P.zlength);
     } else {
         g->P.compensation_pressure = 0;
     }

@@ -20,6 +20,37 @@
 
 namespace des {
 
+// ref_pressure (matprops.cxx:523-535): rho0[0] g depth, or the pressure of the
+// PREM model interpolated in depth (option 1, matprops.cxx:20-62) or of PREM
+// with an average continental crust (option 2, matprops.cxx:66-108); 0 above
+// the surface.  Depths every 100 m and pressures every 1e7 Pa, as integers.
+__host__ __device__ inline double ref_pressure(int option, double rho0, double gravity, double z)
+{
+    const double depth = -z;
+    if (option == 0) return rho0 * gravity * depth;
+    const int km_x10[46] = {0,     30,    150,   244,   400,   600,   800,   1150,  1500,  1850,
+                            2200,  2650,  3100,  3550,  4000,  4500,  5000,  5500,  6000,  6350,
+                            6700,  7210,  7710,  8710,  9710,  10710, 11710, 12710, 13710, 14710,
+                            15710, 16710, 17710, 18710, 19710, 20710, 21710, 22710, 23710, 24710,
+                            25710, 26710, 27410, 27710, 28710, 28910};
+    const int kbar_x10[46] = {0,     3,     33,    60,    112,   178,   245,   361,   478,   594,
+                              711,   864,   1020,  1177,  1335,  1522,  1713,  1907,  2104,  2243,
+                              2383,  2607,  2829,  3276,  3728,  4186,  4648,  5116,  5589,  6068,
+                              6552,  7041,  7535,  8036,  8543,  9056,  9576,  10103, 10638, 11182,
+                              11734, 12297, 12697, 12870, 13456, 13575};
+    // the crust of option 2: 0.82, 4.1 and 6.7 kbar at 3, 15 and 24.4 km
+    const int crust_x100[3] = {82, 410, 670};
+    if (depth <= 0) return 0;
+    int n = 1;
+    while (n < 45 && depth > km_x10[n] * 100.0) ++n;
+    auto press = [&](int i) {
+        if (option == 2 && i >= 1 && i <= 3) return crust_x100[i - 1] * 1e6;
+        return kbar_x10[i] * 1e7;
+    };
+    const double d0 = km_x10[n - 1] * 100.0, d1 = km_x10[n] * 100.0;
+    return press(n - 1) + (press(n) - press(n - 1)) * (depth - d0) / (d1 - d0);
+}
+
 struct Consts {
     MatTable M;
     double gravity, damping_factor, surface_temperature, dt_fraction, fixed_dt;
@@ -30,6 +61,7 @@ struct Consts {
     int elastic_foundation;     // the bottom restoring force of apply_stress_bcs
     int surface_process_option;
     double surface_diffusivity;
+    int ref_pressure_option;
     int damping_option, is_qs, thermal, rheol;
     int vbc_types[10];
     double vbc_values[10];
@@ -659,7 +691,7 @@ __global__ void k_stress_bc_facets(Dev d)
         p = 0;
         if (zcenter < 0) p = 1030 * K.gravity * (0 - zcenter);
     } else {
-        p = K.rho0_0 * K.gravity * (-zcenter);    // ref_pressure (matprops.cxx:523-535)
+        p = ref_pressure(K.ref_pressure_option, K.rho0_0, K.gravity, zcenter);
     }
     for (int j = 0; j < 3; ++j) b.val[j * b.nbf + k] = p * normal[j] / 3;
 }
@@ -912,18 +944,19 @@ __global__ void k_dt(Dev d)
     dt_reduce_and_finalize(d, minh, dtd, live, gridDim.x);
 }
 
-// ic.cxx:100-131 (ref_pressure_option 0)
+// ic.cxx:100-131
 __global__ void k_init_stress(Dev d)
 {
     int e = gtid();
     if (e >= d.nelem) return;
     const size_t E = d.nelem;
     const Consts &K = *d.K;
-    double ks = K.M.mix[d.mix[0]].bulkm;
+    // bulkm(0), or the element's own with a PREM reference pressure
+    const double ks = K.M.mix[d.mix[K.ref_pressure_option != 0 ? e : 0]].bulkm;
     double zn[4];
     load_nodal4(d.z, d.conn[e], zn);
     double zcenter = elem_mean4(zn[0], zn[1], zn[2], zn[3]);
-    double p = K.rho0_0 * K.gravity * (-zcenter);
+    double p = ref_pressure(K.ref_pressure_option, K.rho0_0, K.gravity, zcenter);
     for (int i = 0; i < 3; ++i) {
         d.stress[i * E + e] = -p;
         d.strain[i * E + e] = -p / ks / 3;

@@ -786,17 +786,17 @@ __global__ void kf_vbcs(DevF d)
     d.vz[n] = v[2];
 }
 
-// ic.cxx:100-131 (ref_pressure_option 0), evaluated in FP64
+// ic.cxx:100-131, evaluated in FP64
 __global__ void kf_init_stress(DevF d)
 {
     int e = gtid();
     if (e >= d.nelem) return;
     const size_t E = d.nelem;
     const Consts &K = *d.K;
-    double ks = K.M.mix[d.mix[0]].bulkm;
+    const double ks = K.M.mix[d.mix[K.ref_pressure_option != 0 ? e : 0]].bulkm;
     int4 c = d.conn[e];
     double zc = elem_mean4(__ldg(d.z + c.x), __ldg(d.z + c.y), __ldg(d.z + c.z), __ldg(d.z + c.w));
-    double p = K.rho0_0 * K.gravity * (-zc);
+    double p = ref_pressure(K.ref_pressure_option, K.rho0_0, K.gravity, zc);
     d.s0[e] = -p;
     for (int i = 0; i < 3; ++i) {
         d.stress[i * E + e] = 0.f;

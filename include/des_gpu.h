@@ -33,7 +33,7 @@ extern "C" {
 #define DES_ERR_ARG         2   /* bad pointer, size or mask */
 #define DES_ERR_CUDA        3   /* a CUDA runtime call failed */
 #define DES_ERR_NOMEM       4   /* device allocation failed */
-#define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / PREM reference pressure / closure preconditions */
+#define DES_ERR_UNSUPPORTED 5   /* 2D / plane strain / closure preconditions */
 #define DES_ERR_SIZE        6   /* size above a fixed limit of the entry point */
 #define DES_ERR_DT         11   /* dt <= 0 (geometry.cxx:321-325) or NaN/Inf coordinates (output.cxx:195-208) */
 #define DES_ERR_TOPOLOGY   12   /* a segment is on no element (mesh.cxx:1676-1678) */

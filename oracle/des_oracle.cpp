@@ -377,9 +377,42 @@ void jaumann(double *s, double dt, double w3, double w4, double w5)
 }
 
 // matprops.cxx:523-535, option 0 (lithostatic); the PREM options are not restated
+// matprops.cxx:20-108: the pressure of the PREM model (kbar -> 1e8 Pa) at
+// tabulated depths, linearly interpolated; `modified` takes the average
+// continental crust of option 2 for the top three depths
+double prem_pressure(double depth, bool modified)
+{
+    static const double km[46] = {0,    3,    15,   24.4, 40,   60,   80,   115,  150,  185,  220,  265,
+                                  310,  355,  400,  450,  500,  550,  600,  635,  670,  721,  771,  871,
+                                  971,  1071, 1171, 1271, 1371, 1471, 1571, 1671, 1771, 1871, 1971, 2071,
+                                  2171, 2271, 2371, 2471, 2571, 2671, 2741, 2771, 2871, 2891};
+    static const double kbar[46] = {0,      0.3,    3.3,    6.0,    11.2,   17.8,   24.5,   36.1,   47.8,
+                                    59.4,   71.1,   86.4,   102.0,  117.7,  133.5,  152.2,  171.3,  190.7,
+                                    210.4,  224.3,  238.3,  260.7,  282.9,  327.6,  372.8,  418.6,  464.8,
+                                    511.6,  558.9,  606.8,  655.2,  704.1,  753.5,  803.6,  854.3,  905.6,
+                                    957.6,  1010.3, 1063.8, 1118.2, 1173.4, 1229.7, 1269.7, 1287.0, 1345.6,
+                                    1357.5};
+    static const double crust[3] = {0.82, 4.1, 6.7};
+    // the reference writes each value as a literal (3e3, 0.3e8, ...); the
+    // products below are exact for every entry, so they are the same doubles
+    auto d = [](int i) { return std::round(km[i] * 10) * 100.0; };
+    auto p = [&](int i) {
+        return (modified && i >= 1 && i <= 3) ? std::round(crust[i - 1] * 100) * 1e6 : std::round(kbar[i] * 10) * 1e7;
+    };
+    if (depth <= 0) return 0;
+    int n;
+    for (n = 1; n < 46; n++)
+        if (depth <= d(n)) break;
+    if (n == 46) n = 45;
+    return p(n - 1) + (p(n) - p(n - 1)) * (depth - d(n - 1)) / (d(n) - d(n - 1));
+}
+
+// matprops.cxx:523-535
 double ref_pressure(const des_params &P, double z)
 {
     double depth = -z;
+    if (P.ref_pressure_option == 1) return prem_pressure(depth, false);
+    if (P.ref_pressure_option == 2) return prem_pressure(depth, true);
     return P.rho0.v[0] * P.gravity * depth;
 }
 
@@ -1294,7 +1327,7 @@ int dso_init_fields(dso *o, des_state_view *st)
     if (P.gravity == 0) {
         o->P.compensation_pressure = 0;
     } else {
-        if (P.ref_pressure_option != 0) return DES_ERR_UNSUPPORTED;
+        if (P.ref_pressure_option < 0 || P.ref_pressure_option > 2) return DES_ERR_OPTION;
         double ks = o->bulkm(0);
         for (int e = 0; e < o->nelem; ++e) {
             const int *c = &o->conn[4 * (size_t)e];
@@ -1302,6 +1335,7 @@ int dso_init_fields(dso *o, des_state_view *st)
             for (int i = 0; i < 4; ++i) zcenter += st->coord[3 * (size_t)c[i] + 2];
             zcenter /= 4;
             double p = ref_pressure(P, zcenter);
+            if (P.ref_pressure_option == 1 || P.ref_pressure_option == 2) ks = o->bulkm(e);
             for (int i = 0; i < 3; ++i) {
                 st->stress[6 * (size_t)e + i] = -p;
                 st->strain[6 * (size_t)e + i] = -p / ks / 3;

@@ -98,6 +98,14 @@ OPTION_VARIANTS = {
     # top surface, and the custom-rule template
     "surface": _variant("surface", params=dict(surface_process_option=1, surface_diffusivity=1.0)),
     "surface_custom": _variant("surface_custom", params=dict(surface_process_option=101)),
+    # PREM reference pressure (matprops.cxx:20-108, 523-535) in the initial
+    # stress, the compensation pressure and the tractions of a free side wall
+    "prem": _variant("prem", params=dict(ref_pressure_option=1),
+                     vbc=([0, 1, 1, 1, 1, 0, 0, 0, 0, 0], [0.0, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    "prem_crust": _variant("prem_crust", nlayers=3, layer_rho0=(2800.0, 3000.0, 3300.0),
+                           layer_depths=(0.3, 0.6), params=dict(ref_pressure_option=2),
+                           mats=dict(bulk_modulus=[100e9, 128e9, 150e9]),
+                           vbc=([0, 1, 1, 1, 1, 0, 0, 0, 0, 0], [0.0, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
     "mats16": _variant("mats16", nz=6, nlayers=16,
                        layer_rho0=tuple(2700.0 + 40.0 * k for k in range(16)),
                        layer_depths=tuple((k + 1) / 16 for k in range(15)),
