@@ -175,6 +175,13 @@ class Mesh:
         self.segflag = np.zeros(self.nseg, np.int32)
         abi.check(lib.des_box_fill(C.byref(spec), abi.dptr(self.coord), abi.iptr(self.connectivity),
                                    abi.iptr(self.segment), abi.iptr(self.segflag)), "des_box_fill")
+        # inclined x sides: the box sheared in x along z, its x faces flagged as
+        # the inclined boundaries n0 and n1 (bcflag bits 6 and 7)
+        shear = cfg.extra.get("shear_xz", 0.0)
+        if shear:
+            self.coord[:, 0] += shear * self.coord[:, 2]
+            self.segflag[self.segflag == 1] = 1 << 6
+            self.segflag[self.segflag == 2] = 1 << 7
         self.nmat = cfg.nlayers
         self.elemmarkers = np.zeros((self.nelem, self.nmat), np.int32)
         mattypes = np.arange(cfg.nlayers, dtype=np.int32)

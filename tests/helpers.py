@@ -39,7 +39,7 @@ def layered_config(nx=6, ny=5, nz=6):
 
 
 def _variant(name, nx=6, ny=5, nz=3, base="1", rheology=None, params=None, mats=None, vbc=None,
-             **cfg_kw):
+             shear_xz=0.0, **cfg_kw):
     cfg = W.scaled(W.CONFIGS[base], nx, ny, nz, name=f"opt_{name}_{nx}x{ny}x{nz}")
     if rheology:
         cfg.rheology = rheology
@@ -52,6 +52,8 @@ def _variant(name, nx=6, ny=5, nz=3, base="1", rheology=None, params=None, mats=
         extra["mats"] = dict(extra.get("mats", {}), **mats)
     if vbc:
         extra["vbc_types"], extra["vbc_values"] = vbc
+    if shear_xz:
+        extra["shear_xz"] = shear_xz
     cfg.extra = extra
     return cfg
 
@@ -106,6 +108,16 @@ OPTION_VARIANTS = {
                            layer_depths=(0.3, 0.6), params=dict(ref_pressure_option=2),
                            mats=dict(bulk_modulus=[100e9, 128e9, 150e9]),
                            vbc=([0, 1, 1, 1, 1, 0, 0, 0, 0, 0], [0.0, 0.01 / _YR, 0.0, 0.0, 0.0, 0.0, 0, 0, 0, 0])),
+    # inclined sides n0, n1 (the box sheared, its x faces flagged inclined):
+    # normal velocity (type 1, with the edge rule where they meet y and z
+    # sides), velocity along the normal (3), horizontal normal velocity (11),
+    # horizontal velocity along the normal (13)
+    "inclined_1": _variant("inclined_1", shear_xz=0.3, vbc=([0, 0, 1, 1, 1, 0, 1, 1, 0, 0],
+                                              [0.0, 0.0, 0.0, 0.0, 0.0, 0.0, -0.01 / _YR, 0.01 / _YR, 0, 0])),
+    "inclined_3_11": _variant("inclined_3_11", shear_xz=0.3, vbc=([0, 0, 1, 1, 1, 0, 3, 11, 0, 0],
+                                                    [0.0, 0.0, 0.0, 0.0, 0.0, 0.0, -0.01 / _YR, 0.01 / _YR, 0, 0])),
+    "inclined_13": _variant("inclined_13", shear_xz=0.3, vbc=([0, 0, 1, 1, 1, 0, 13, 1, 0, 0],
+                                                [0.0, 0.0, 0.0, 0.0, 0.0, 0.0, -0.01 / _YR, 0.01 / _YR, 0, 0])),
     "mats16": _variant("mats16", nz=6, nlayers=16,
                        layer_rho0=tuple(2700.0 + 40.0 * k for k in range(16)),
                        layer_depths=tuple((k + 1) / 16 for k in range(15)),
