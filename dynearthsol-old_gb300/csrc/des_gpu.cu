@@ -62,6 +62,7 @@ struct des_gpu {
     double *dl = nullptr;                 // host-layout rows of an overlapped download
     long long dl_elems = 0;
     cudaEvent_t head_done = nullptr;      // a step's passes before E-A are done
+    cudaEvent_t up_done = nullptr;        // the copy stream's uploads are done
     cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
     int avg_interval = 0;                 // Output::average_fields every step when > 0
     double *avg_c0 = nullptr, *avg_strain0 = nullptr, *avg_stress = nullptr, *avg_dpls = nullptr,
@@ -648,6 +649,7 @@ int ensure_copy_stream(des_gpu *g)
 {
     if (!g->copy_stream) DES_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
     if (!g->head_done) DES_CUDA(cudaEventCreateWithFlags(&g->head_done, cudaEventDisableTiming));
+    if (!g->up_done) DES_CUDA(cudaEventCreateWithFlags(&g->up_done, cudaEventDisableTiming));
     return DES_OK;
 }
 
@@ -903,6 +905,7 @@ int des_gpu_destroy(des_gpu *g)
     }
     if (g->snap_ready) cudaEventDestroy(g->snap_ready);
     if (g->head_done) cudaEventDestroy(g->head_done);
+    if (g->up_done) cudaEventDestroy(g->up_done);
     if (g->snap_done) cudaEventDestroy(g->snap_done);
     if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->graph) cudaGraphExecDestroy(g->graph);
@@ -1632,6 +1635,75 @@ constexpr unsigned kFinishedAfterPass[5] = {
 constexpr unsigned kBeforeLastPass = kFinishedAfterPass[0] | kFinishedAfterPass[1] | kFinishedAfterPass[2] |
                                      kFinishedAfterPass[3] | kFinishedAfterPass[4];
 
+// One element field of the overlapped upload: its host rows and where they go.
+struct UpPart {
+    const double *host;
+    int ncomp;
+    double *dst64;
+    float *dst32;
+    bool stress_split;
+};
+
+static std::vector<UpPart> up_parts(des_gpu *g, const des_state_view *h, unsigned later)
+{
+    const bool f32 = g->prec == DES_PREC_FP32;
+    std::vector<UpPart> out;
+    out.push_back({h->volume_old, 1, g->d.vol_old, nullptr, false});
+    if (later & DES_F_STRESS) out.push_back({h->stress, 6, g->d.stress, nullptr, false});
+    if (later & DES_F_STRAIN)
+        out.push_back({h->strain, 6, f32 ? nullptr : g->d.strain, f32 ? g->f.strain : nullptr, false});
+    if (later & DES_F_PLSTRAIN) {
+        out.push_back({h->plstrain, 1, g->d.pls, nullptr, false});
+        out.push_back({h->delta_plstrain, 1, f32 ? nullptr : g->d.dpls, f32 ? g->f.dpls : nullptr, false});
+    }
+    return out;
+}
+
+// the host rows of volume_old and the `later` fields into the download
+// buffer (sized here for this call's downloads too, `down` doubles), by the
+// copy engine on the copy stream
+static int upload_elements_async(des_gpu *g, const des_state_view *h, unsigned later, long long down)
+{
+    const long long E = g->nelem;
+    std::vector<UpPart> parts = up_parts(g, h, later);
+    long long need = 0;
+    for (const UpPart &q : parts) {
+        if (!q.host) return DES_ERR_ARG;
+        need += q.ncomp * E;
+    }
+    int rc;
+    if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, std::max(need, down)))) return rc;
+    // the buffer's previous contents have left on the copy stream
+    DES_CUDA(cudaStreamSynchronize(g->copy_stream));
+    long long off = 0;
+    for (const UpPart &q : parts) {
+        DES_CUDA(cudaMemcpyAsync(g->dl + off, q.host, sizeof(double) * q.ncomp * E, cudaMemcpyHostToDevice,
+                                 g->copy_stream));
+        off += q.ncomp * E;
+    }
+    DES_CUDA(cudaEventRecord(g->up_done, g->copy_stream));
+    return DES_OK;
+}
+
+// the uploaded rows into the device's arrays, once the copies are done
+static int finish_elements_async(des_gpu *g, const des_state_view *h, unsigned later)
+{
+    const long long E = g->nelem;
+    DES_CUDA(cudaStreamWaitEvent(g->stream, g->up_done, 0));
+    long long off = 0;
+    for (const UpPart &q : up_parts(g, h, later)) {
+        const double *src = g->dl + off;
+        if (q.dst64)
+            k_aos_to_soa<<<blocks(E * q.ncomp, 256), 256, 0, g->stream>>>(src, q.dst64, q.ncomp, E, 0, E);
+        else
+            k_aos_to_soa_f<<<blocks(E * q.ncomp, 256), 256, 0, g->stream>>>(src, q.dst32, q.ncomp, E, 0, E);
+        DES_LAUNCH();
+        off += q.ncomp * E;
+    }
+    g->primed = false;
+    return DES_OK;
+}
+
 // volume, shape derivatives and nodal masses from the device's coordinates
 // and temperature, the values update_mesh (dynearthsol.cxx:237-261) leaves
 static int derive_geometry(des_gpu *g)
@@ -1667,12 +1739,22 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
     const unsigned derived = DES_F_VOLUME | DES_F_SHAPE | DES_F_MASS;
     const bool derive = (up & DES_F_COORD) && (up & DES_F_TEMPERATURE) && (up & derived) == derived;
     if (derive) up &= ~derived;
-    int rc = des_gpu_upload(g, host, up);
+    // while the geometry is derived, the element fields it does not read come
+    // over the copy engine on the second stream (the FP32 form's derivation
+    // reads the reference stress, so its stress is uploaded first)
+    unsigned later = 0;
+    if (derive) later = up & (DES_F_STRAIN | DES_F_PLSTRAIN | (g->prec == DES_PREC_FP64 ? DES_F_STRESS : 0u));
+    int rc = des_gpu_upload(g, host, up & ~later);
     if (rc) return rc;
     if (derive) {
-        if (host->nelem != g->nelem) return DES_ERR_ARG;
-        if ((rc = upload_field(g, host->volume_old, g->d.vol_old, 1, g->nelem))) return rc;
+        if (host->nelem != g->nelem || !host->volume_old) return DES_ERR_ARG;
+        std::vector<DownPart> all;
+        if ((rc = down_parts(g, host, mask, all))) return rc;
+        long long down = 0;
+        for (const DownPart &q : all) down += q.ncomp * q.rows;
+        if ((rc = upload_elements_async(g, host, later, down))) return rc;
         if ((rc = derive_geometry(g))) return rc;
+        if ((rc = finish_elements_async(g, host, later))) return rc;
     }
     if (nsteps == 0) return des_gpu_download(g, host, mask);
     // every step but the last as the graph; the last as its passes, so that
