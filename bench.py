@@ -301,6 +301,44 @@ def yielding_forms(args, local, world, barrier, reduce, compare):
     return out
 
 
+def accuracy_2000(cfg_key, box, local, compare):
+    """FP32 form against FP64 form after 500, 1,000 and 2,000 steps from init on
+    the bench workload with damping option 2 (smooth: a 1e-12 perturbation of
+    the FP64 loop stays bounded), each form timed as it runs."""
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+    base = W.CONFIGS[cfg_key]
+    if box:
+        nx, ny, nz = (int(v) for v in box.lower().split("x"))
+        base = W.scaled(base, nx, ny, nz)
+    d = dict(base.__dict__)
+    d["extra"] = dict(base.extra, params=dict(base.extra.get("params", {}), damping_option=2))
+    cfg = W.Config(**d)
+    mesh, p, T, pls, _ = D.setup_case(cfg)
+    states, secs = {}, {}
+    for name, prec in (("fp64", abi.PREC_FP64), ("fp32", abi.PREC_FP32)):
+        q = abi.Params.from_buffer_copy(p)
+        q.precision = prec
+        dev = D.Device(mesh, q, device=local)
+        s = W.new_state(mesh, T, pls)
+        dev.upload(s, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dev.init_fields()
+        done, t = 0, 0.0
+        for k in (500, 1000, 2000):
+            t -= time.perf_counter()
+            dev.step(k - done)
+            dev.report()
+            t += time.perf_counter()
+            done = k
+            states[(name, k)] = dev.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
+        secs[name] = t
+        dev.close()
+    out = {"workload": f"{cfg.name} with damping option 2", "seconds_for_2000_steps": secs}
+    for k in (500, 1000, 2000):
+        out[f"fp32_vs_fp64_after_{k}_steps"] = compare(states[("fp32", k)], states[("fp64", k)])
+    return out
+
+
 def large_case_forms(args, local, world, reduce):
     """Config 5 (400x400x80 hexes x 6 = 76.8M tets, three material layers,
     elasto-visco-plastic): both forms, their device footprint and rate."""
@@ -445,6 +483,8 @@ def run_ours(args):
     if not args.no_yielding:
         forms["yielding"] = yielding_forms(args, local, world, barrier,
                                            torch_reduce_max(f"cuda:{local}") if dist else None, compare)
+    if not args.no_accuracy and world == 1:
+        forms["fp32_accuracy_2000_steps"] = accuracy_2000(args.config, args.box, local, compare)
     if not args.no_large:
         forms["config5"] = large_case_forms(args, local, world,
                                             torch_reduce_max(f"cuda:{local}") if dist else None)
@@ -583,6 +623,8 @@ def main():
     ap.add_argument("--no-yielding", action="store_true",
                     help="skip the forms on the yielding workload")
     ap.add_argument("--no-large", action="store_true", help="skip config 5 (76.8M tets)")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the 2,000-step FP32-against-FP64 accuracy run")
     ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure"], default=None,
                     help="run one form alone on --config/--box (for profiling)")
     ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
