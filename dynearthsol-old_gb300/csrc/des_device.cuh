@@ -12,6 +12,8 @@
 
 #include <cstdint>
 
+#include "des_softf64.cuh"
+
 namespace des {
 
 constexpr double kDeg2Rad = 3.1415926535897932384626433832795 / 180;   // constants.hpp:76
@@ -683,17 +685,18 @@ __device__ __forceinline__ void spin_and_rate(const double V[4][3], const double
                                               const double *dz, double &w3, double &w4, double &w5,
                                               double D[6])
 {
+    // the products on the integer pipes (sf::mul rounds as the FP64 unit does)
     D[0] = 0;
-    for (int i = 0; i < 4; ++i) D[0] += V[i][0] * dx[i];
+    for (int i = 0; i < 4; ++i) D[0] += sf::mul(V[i][0], dx[i]);
     D[1] = 0;
-    for (int i = 0; i < 4; ++i) D[1] += V[i][1] * dy[i];
+    for (int i = 0; i < 4; ++i) D[1] += sf::mul(V[i][1], dy[i]);
     D[2] = 0;
-    for (int i = 0; i < 4; ++i) D[2] += V[i][2] * dz[i];
+    for (int i = 0; i < 4; ++i) D[2] += sf::mul(V[i][2], dz[i]);
     double t3 = 0, t4 = 0, t5 = 0, u3 = 0, u4 = 0, u5 = 0;
     for (int i = 0; i < 4; ++i) {
-        const double xy = V[i][0] * dy[i], yx = V[i][1] * dx[i];
-        const double xz = V[i][0] * dz[i], zx = V[i][2] * dx[i];
-        const double yz = V[i][1] * dz[i], zy = V[i][2] * dy[i];
+        const double xy = sf::mul(V[i][0], dy[i]), yx = sf::mul(V[i][1], dx[i]);
+        const double xz = sf::mul(V[i][0], dz[i]), zx = sf::mul(V[i][2], dx[i]);
+        const double yz = sf::mul(V[i][1], dz[i]), zy = sf::mul(V[i][2], dy[i]);
         t3 += xy + yx;
         u3 += xy - yx;
         t4 += xz + zx;
@@ -714,15 +717,16 @@ __device__ __forceinline__ void spin_and_rate(const double V[4][3], const double
 // sum (exact, as above)
 __device__ __forceinline__ void jaumann64(double *s, double dt, double w3, double w4, double w5)
 {
-    const double p3 = s[3] * w3, p4 = s[4] * w4, p5 = s[5] * w5;
+    // (products on the integer pipes, sf::mul)
+    const double p3 = sf::mul(s[3], w3), p4 = sf::mul(s[4], w4), p5 = sf::mul(s[5], w5);
     double inc[6];
     inc[0] = 2.0 * (-p3 - p4);
     inc[1] = 2.0 * (p3 - p5);
     inc[2] = 2.0 * (p4 + p5);
-    inc[3] = s[0] * w3 - s[1] * w3 - s[4] * w5 - s[5] * w4;
-    inc[4] = s[0] * w4 - s[2] * w4 + s[3] * w5 - s[5] * w3;
-    inc[5] = s[1] * w5 - s[2] * w5 + s[3] * w4 + s[4] * w3;
-    for (int i = 0; i < 6; ++i) s[i] += dt * inc[i];
+    inc[3] = sf::mul(s[0], w3) - sf::mul(s[1], w3) - sf::mul(s[4], w5) - sf::mul(s[5], w4);
+    inc[4] = sf::mul(s[0], w4) - sf::mul(s[2], w4) + sf::mul(s[3], w5) - sf::mul(s[5], w3);
+    inc[5] = sf::mul(s[1], w5) - sf::mul(s[2], w5) + sf::mul(s[3], w4) + sf::mul(s[4], w3);
+    for (int i = 0; i < 6; ++i) s[i] += sf::mul(dt, inc[i]);
 }
 
 // fields.cxx:419-433
@@ -745,16 +749,17 @@ __device__ __forceinline__ void jaumann(R *s, R dt, R w3, R w4, R w5)
 __device__ __forceinline__ void conduction(const double *dx, const double *dy, const double *dz,
                                            const double Tn[4], double kv, double tr[4])
 {
+    // (products on the integer pipes, sf::mul)
     double D[4][4];
     for (int i = 0; i < 4; ++i)
         for (int j = i; j < 4; ++j) {
-            D[i][j] = dx[i] * dx[j] + dy[i] * dy[j] + dz[i] * dz[j];
+            D[i][j] = sf::mul(dx[i], dx[j]) + sf::mul(dy[i], dy[j]) + sf::mul(dz[i], dz[j]);
             D[j][i] = D[i][j];
         }
     for (int i = 0; i < 4; ++i) {
         double diffusion = 0.;
-        for (int j = 0; j < 4; ++j) diffusion += D[i][j] * Tn[j];
-        tr[i] = diffusion * kv;
+        for (int j = 0; j < 4; ++j) diffusion += sf::mul(D[i][j], Tn[j]);
+        tr[i] = sf::mul(diffusion, kv);
     }
 }
 

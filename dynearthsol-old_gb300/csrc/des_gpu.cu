@@ -682,9 +682,62 @@ int capture_step_graph(des_gpu *g)
     return cuda_rc(e);
 }
 
+__device__ __forceinline__ unsigned long long check_mix(unsigned long long z)
+{
+    z += 0x9e3779b97f4a7c15ull;
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+// sf::mul and sf::to_float against the FP64 unit's multiply and conversion
+__global__ void k_softf64_check(unsigned long long *bad, long long n, unsigned long long seed)
+{
+    unsigned long long nb[4] = {0, 0, 0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long r1 = check_mix(seed + 2 * i + 1), r2 = check_mix(seed + 2 * i + 2);
+        const unsigned long long keep = 0x800fffffffffffffull;
+        const double x = sf::from_bits(r1), y = sf::from_bits(r2);
+        const double x1 = sf::from_bits((r1 & keep) | ((963ull + r2 % 121) << 52));
+        const double y1 = sf::from_bits((r2 & keep) | ((963ull + (r1 >> 7) % 121) << 52));
+        const double xf = sf::from_bits((r1 & keep) | ((870ull + (r2 >> 11) % 310) << 52));
+        double h = __dmul_rn(x, y), g = sf::mul(x, y);
+        nb[0] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __dmul_rn(x1, y1);
+        g = sf::mul(x1, y1);
+        nb[1] += sf::bits(h) != sf::bits(g);
+        float hf = __double2float_rn(x), gf = sf::to_float(x);
+        nb[2] += __float_as_uint(hf) != __float_as_uint(gf) && !(hf != hf && gf != gf);
+        hf = __double2float_rn(xf);
+        gf = sf::to_float(xf);
+        nb[3] += __float_as_uint(hf) != __float_as_uint(gf);
+    }
+    for (int k = 0; k < 4; ++k)
+        if (nb[k]) atomicAdd(bad + k, nb[k]);
+}
+
 }  // namespace
 
 extern "C" {
+
+int des_gpu_softf64_check(int device, long long n, unsigned long long seed, unsigned long long mismatches[4])
+{
+    if (n < 0 || !mismatches) return DES_ERR_ARG;
+    DES_CUDA(cudaSetDevice(device));
+    unsigned long long *bad = nullptr;
+    DES_CUDA(cudaMalloc(&bad, 4 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
+    int sms = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) {
+        k_softf64_check<<<sms * 8, 256>>>(bad, n, seed);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, bad, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    cudaFree(bad);
+    return cuda_rc(e);
+}
 
 const char *des_gpu_error_string(int code)
 {

@@ -118,8 +118,8 @@ __device__ __forceinline__ void f_store6(float *a, size_t E, int e, const float 
 // element mean temperature in FP32 (from the FP64 accumulator)
 __device__ __forceinline__ float f_elem_T(const DevF &d, int4 c)
 {
-    return elem_mean4((float)__ldg(d.T + c.x), (float)__ldg(d.T + c.y), (float)__ldg(d.T + c.z),
-                      (float)__ldg(d.T + c.w));
+    return elem_mean4(sf::to_float(__ldg(d.T + c.x)), sf::to_float(__ldg(d.T + c.y)),
+                      sf::to_float(__ldg(d.T + c.z)), sf::to_float(__ldg(d.T + c.w)));
 }
 
 // matprops.cxx:707-728 in FP32
@@ -328,8 +328,8 @@ __device__ __forceinline__ void f_next_contrib(const DevF &d, int e, int4 c, con
         // conduction vector kv (grad N_i . grad T) with grad T from temperature
         // differences (sum_j grad N_j = 0), differences taken in FP64
         double T0 = __ldg(d.T + c.x);
-        float t1 = (float)(__ldg(d.T + c.y) - T0), t2 = (float)(__ldg(d.T + c.z) - T0),
-              t3 = (float)(__ldg(d.T + c.w) - T0);
+        float t1 = sf::to_float(__ldg(d.T + c.y) - T0), t2 = sf::to_float(__ldg(d.T + c.z) - T0),
+              t3 = sf::to_float(__ldg(d.T + c.w) - T0);
         float gx = dx[1] * t1 + dx[2] * t2 + dx[3] * t3;
         float gy = dy[1] * t1 + dy[2] * t2 + dy[3] * t3;
         float gz = dz[1] * t1 + dz[2] * t2 + dz[3] * t3;
@@ -353,17 +353,19 @@ __device__ __forceinline__ double f_cofactors(const double X[4][3], double cf[4]
     }
     // (fused multiply-adds: this form is held to a tolerance, not to the
     // reference's rounding)
-    cf[1][0] = fma(b[1], q[2], -b[2] * q[1]);
-    cf[1][1] = fma(b[2], q[0], -b[0] * q[2]);
-    cf[1][2] = fma(b[0], q[1], -b[1] * q[0]);
-    cf[2][0] = fma(q[1], a[2], -q[2] * a[1]);
-    cf[2][1] = fma(q[2], a[0], -q[0] * a[2]);
-    cf[2][2] = fma(q[0], a[1], -q[1] * a[0]);
-    cf[3][0] = fma(a[1], b[2], -a[2] * b[1]);
-    cf[3][1] = fma(a[2], b[0], -a[0] * b[2]);
-    cf[3][2] = fma(a[0], b[1], -a[1] * b[0]);
+    // (the plain products on the integer pipes, sf::mul, rounded as the FP64
+    // unit rounds them)
+    cf[1][0] = fma(b[1], q[2], -sf::mul(b[2], q[1]));
+    cf[1][1] = fma(b[2], q[0], -sf::mul(b[0], q[2]));
+    cf[1][2] = fma(b[0], q[1], -sf::mul(b[1], q[0]));
+    cf[2][0] = fma(q[1], a[2], -sf::mul(q[2], a[1]));
+    cf[2][1] = fma(q[2], a[0], -sf::mul(q[0], a[2]));
+    cf[2][2] = fma(q[0], a[1], -sf::mul(q[1], a[0]));
+    cf[3][0] = fma(a[1], b[2], -sf::mul(a[2], b[1]));
+    cf[3][1] = fma(a[2], b[0], -sf::mul(a[0], b[2]));
+    cf[3][2] = fma(a[0], b[1], -sf::mul(a[1], b[0]));
     for (int k = 0; k < 3; ++k) cf[0][k] = -(cf[1][k] + cf[2][k] + cf[3][k]);
-    return fma(a[0], cf[1][0], fma(a[1], cf[1][1], a[2] * cf[1][2]));     // 6 V
+    return fma(a[0], cf[1][0], fma(a[1], cf[1][1], sf::mul(a[2], cf[1][2])));     // 6 V
 }
 
 // FP64 part of the element force vectors for the next step: s0 grad(N_i) V
@@ -372,11 +374,11 @@ __device__ __forceinline__ double f_cofactors(const double X[4][3], double cf[4]
 __device__ __forceinline__ void f_reference_force(const DevF &d, int e, const double cf[4][3], double vol)
 {
     const size_t E = d.nelem;
-    const double s6 = d.s0[e] * (1.0 / 6.0);
-    const double buoy = d.F->gravity != 0.f ? d.F->mix[d.mix[e]].rho_g4 * vol : 0.0;
+    const double s6 = sf::mul(d.s0[e], 1.0 / 6.0);
+    const double buoy = d.F->gravity != 0.f ? sf::mul(d.F->mix[d.mix[e]].rho_g4, vol) : 0.0;
     for (int i = 0; i < 4; ++i) {
-        d.f0[(i)*E + e] = s6 * cf[i][0];
-        d.f0[(i + 4) * E + e] = s6 * cf[i][1];
+        d.f0[(i)*E + e] = sf::mul(s6, cf[i][0]);
+        d.f0[(i + 4) * E + e] = sf::mul(s6, cf[i][1]);
         d.f0[(i + 8) * E + e] = fma(s6, cf[i][2], buoy);
     }
 }
@@ -634,7 +636,7 @@ __device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, float
     f_load_xyz4(d, c, X);
     double cf[4][3];
     const double det = f_cofactors(X, cf);
-    const double vol = det * (1.0 / 6.0);
+    const double vol = sf::mul(det, 1.0 / 6.0);
     f_reference_force(d, e, cf, vol);
     if (c2max) {
         double m = 0;
@@ -642,11 +644,11 @@ __device__ __forceinline__ double f_geometry(const DevF &d, int e, int4 c, float
         *c2max = m;
     }
     // the gradients themselves are FP32: c_i / (6 V)
-    const float iv = 1.f / (float)det;
+    const float iv = 1.f / sf::to_float(det);
     for (int i = 0; i < 4; ++i) {
-        dx[i] = (float)cf[i][0] * iv;
-        dy[i] = (float)cf[i][1] * iv;
-        dz[i] = (float)cf[i][2] * iv;
+        dx[i] = sf::to_float(cf[i][0]) * iv;
+        dy[i] = sf::to_float(cf[i][1]) * iv;
+        dz[i] = sf::to_float(cf[i][2]) * iv;
         d.shp[(0 + i) * E + e] = dx[i];
         d.shp[(4 + i) * E + e] = dy[i];
         d.shp[(8 + i) * E + e] = dz[i];
@@ -674,7 +676,7 @@ __global__ void kf_fe_a(DevF d, int e0, unsigned nblocks)
         d.vol_old[e] = d.vol[e];
         d.vol[e] = vol;
         if (not_positive(vol)) atomicOr(&d.clk->status, 0x4u);
-        float volf = (float)vol;
+        float volf = sf::to_float(vol);
         d.c_vol[e] = volf;
         const MixF &xf = F.mix[d.mix[e]];
         {

@@ -1,0 +1,207 @@
+// Exactly rounded FP64 multiply and FP64 -> FP32 conversion on the integer
+// pipes.
+//
+// GB300 retires 2 FP64 instructions per clock per SM, while its integer ALU
+// and FMA pipes retire 64 and more lanes per clock.  A kernel bound by the
+// FP64 pipe can move part of its multiplies and conversions to these
+// routines and run both pipes at once.  Each returns, bit for bit, what the
+// FP64 unit returns (IEEE-754 binary64, round to nearest even, subnormals
+// kept): the fast path covers normal operands with a normal result, and the
+// rest (zeros, subnormals, infinities, NaN, overflow, underflow) takes an
+// integer slow path.  Neither path issues an FP64 instruction: the compiler
+// predicates short branches, and a predicated FP64 instruction still
+// occupies the FP64 pipe.  64-bit leading-zero counts are formed from two
+// 32-bit counts for the same reason (the 64-bit count is lowered through a
+// conversion on the FP64 unit).
+//
+// The header compiles as plain C++ too, so that the host can check it
+// against its own IEEE arithmetic.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define DES_SF_HD __host__ __device__ __forceinline__
+#else
+#define DES_SF_HD static inline
+#endif
+
+namespace des {
+namespace sf {
+
+constexpr uint64_t kAbs = 0x7fffffffffffffffull;
+constexpr uint64_t kSign = 0x8000000000000000ull;
+constexpr uint64_t kFrac = 0x000fffffffffffffull;
+constexpr uint64_t kHidden = 0x0010000000000000ull;
+constexpr uint64_t kInf = 0x7ff0000000000000ull;
+constexpr uint64_t kQuiet = 0x0008000000000000ull;
+constexpr uint64_t kDefaultNaN = 0x7ff8000000000000ull;
+
+DES_SF_HD uint64_t bits(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+DES_SF_HD double from_bits(uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+DES_SF_HD float float_from_bits(uint32_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(b);
+#else
+    float x;
+    memcpy(&x, &b, 4);
+    return x;
+#endif
+}
+
+DES_SF_HD int clz32(uint32_t x)
+{
+#if defined(__CUDA_ARCH__)
+    return __clz((int)x);
+#else
+    return x ? __builtin_clz(x) : 32;
+#endif
+}
+
+// leading zeros of a 64-bit word from two 32-bit counts
+DES_SF_HD int clz64(uint64_t x)
+{
+    const uint32_t hi = (uint32_t)(x >> 32);
+    return hi ? clz32(hi) : 32 + clz32((uint32_t)x);
+}
+
+DES_SF_HD uint64_t mulhi64(uint64_t a, uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// round to nearest even on the 11 bits below a 53-bit significand held at
+// the top of r (bit 63 down to 11), then pack with the biased exponent e
+// (1 <= e; a carry out of the significand moves into the exponent, and
+// e = 2046 with a carry gives the infinity the rounding asks for)
+DES_SF_HD uint64_t round_pack(uint64_t sign, int e, uint64_t r)
+{
+    const uint64_t m = r >> 11, rem = r & 0x7ff;
+    const uint64_t up = (uint64_t)((rem > 0x400) | ((rem == 0x400) & (uint32_t)m));
+    return ((((uint64_t)(e - 1)) << 52) + m + up) | sign;
+}
+
+// the cases the fast path of mul leaves: zeros, subnormals, infinities, NaN,
+// results outside the normal range
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__
+#else
+static
+#endif
+uint64_t mul_slow(uint64_t a, uint64_t b)
+{
+    const uint64_t sign = (a ^ b) & kSign;
+    const uint64_t ma = a & kAbs, mb = b & kAbs;
+    const int ea = (int)(ma >> 52), eb = (int)(mb >> 52);
+    if (ea == 2047 || eb == 2047) {
+        if (ma > kInf) return a | kQuiet;
+        if (mb > kInf) return b | kQuiet;
+        if (ma == 0 || mb == 0) return kDefaultNaN;
+        return sign | kInf;
+    }
+    if (ma == 0 || mb == 0) return sign;
+    uint64_t fa = (ma & kFrac) | (ea ? kHidden : 0), fb = (mb & kFrac) | (eb ? kHidden : 0);
+    const int la = clz64(fa), lb = clz64(fb);
+    fa <<= la;
+    fb <<= lb;
+    const uint64_t hi = mulhi64(fa, fb), lo = fa * fb;
+    const int lz = (int)(1 - (hi >> 63));
+    uint64_t r = (hi << lz) | (uint64_t)(lo != 0);
+    int e = (ea ? ea : 1) + (eb ? eb : 1) - 1000 - la - lb - lz;
+    if (e >= 2047) return sign | kInf;
+    if (e < 1) {
+        const uint32_t sh = (uint32_t)(1 - e) > 63u ? 63u : (uint32_t)(1 - e);
+        uint64_t rs = r >> sh;
+        rs |= (uint64_t)((rs << sh) != r);
+        r = rs;
+        e = 1;
+    }
+    return round_pack(sign, e, r);
+}
+
+// x * y as the FP64 unit rounds it.  Fast path: both significands shifted
+// to bit 63; the top 64 bits of their 128-bit product carry the result and
+// the low 64 bits only a sticky bit, which rounds like the exact product
+// because the rounding position is 11 bits above it.
+DES_SF_HD double mul(double x, double y)
+{
+    const uint64_t a = bits(x), b = bits(y);
+    const uint32_t ea = (uint32_t)(a >> 52) & 0x7ff, eb = (uint32_t)(b >> 52) & 0x7ff;
+    if (ea - 1 < 2046u && eb - 1 < 2046u) {
+        const uint64_t fa = ((a & kFrac) | kHidden) << 11, fb = ((b & kFrac) | kHidden) << 11;
+        const uint64_t hi = mulhi64(fa, fb), lo = fa * fb;
+        const int lz = (int)(1 - (hi >> 63));
+        const int e = (int)(ea + eb) - 1022 - lz;
+        if ((uint32_t)(e - 1) < 2046u)
+            return from_bits(round_pack((a ^ b) & kSign, e, (hi << lz) | (uint64_t)(lo != 0)));
+    }
+    // a zero times a finite number (frequent: zero velocity components and
+    // shape-function derivatives) without the call
+    if (((a & kAbs) == 0 && eb != 2047) || ((b & kAbs) == 0 && ea != 2047)) return from_bits((a ^ b) & kSign);
+    return from_bits(mul_slow(a, b));
+}
+
+// the cases the fast path of to_float leaves: zeros, subnormal FP32
+// results, infinities, NaN, overflow
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__
+#else
+static
+#endif
+uint32_t to_float_slow(uint64_t a)
+{
+    const uint32_t sign = (uint32_t)(a >> 32) & 0x80000000u;
+    const int e = (int)((a >> 52) & 0x7ff);
+    if (e == 2047) return (a & kFrac) ? 0x7fffffffu : (sign | 0x7f800000u);
+    if (e - 896 >= 255) return sign | 0x7f800000u;
+    // FP32 subnormal or zero: k = round(significand / 2^(926 - e)) units of 2^-149
+    const int sh = 926 - e;
+    if (sh >= 54) return sign;
+    const uint64_t f = (a & kFrac) | kHidden;
+    const uint64_t k = f >> sh, rem = f & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    const uint64_t up = (uint64_t)((rem > half) | ((rem == half) & (uint32_t)k));
+    return sign | (uint32_t)(k + up);
+}
+
+// (float)x, round to nearest even, as the FP64 unit converts it
+DES_SF_HD float to_float(double x)
+{
+    const uint64_t a = bits(x);
+    const uint32_t hi = (uint32_t)(a >> 32), lo = (uint32_t)a;
+    const int ef = (int)((hi >> 20) & 0x7ff) - 896;
+    if ((uint32_t)(ef - 1) < 254u) {
+        const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+        const uint32_t rem = lo & 0x1fffffffu;
+        const uint32_t up = (uint32_t)((rem > 0x10000000u) | ((rem == 0x10000000u) & m));
+        return float_from_bits((hi & 0x80000000u) | ((((uint32_t)ef) << 23) + m + up));
+    }
+    return float_from_bits(to_float_slow(a));
+}
+
+}  // namespace sf
+}  // namespace des

@@ -64,6 +64,7 @@ def lib():
     L.des_gpu_device_bytes.argtypes = [C.c_void_p]
     L.des_gpu_device_bytes.restype = C.c_longlong
     L.des_gpu_kernels_per_step.argtypes = [C.c_void_p]
+    L.des_gpu_softf64_check.argtypes = [C.c_int, C.c_longlong, C.c_ulonglong, P(C.c_ulonglong)]
     L.des_gpu_time_steps.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     L.des_gpu_profile_steps.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
     L.des_host_register.argtypes = [C.c_void_p, C.c_longlong]
@@ -319,6 +320,16 @@ def write_checkpoint(path, mesh, state, compensation_pressure):
     mv = mesh.view()
     _ck(lib().des_write_checkpoint(str(path).encode(), C.byref(mv), state.time, compensation_pressure,
                                    abi.dptr(state.volume_old)), "des_write_checkpoint")
+
+
+def softf64_check(n, seed=20261203, device=0):
+    """Mismatches of the integer-pipe FP64 multiply and FP64 -> FP32
+    conversion against the device's FP64 unit over n seeded operands per
+    kind: [multiply, any bits; multiply, near 1; conversion, any bits;
+    conversion, FP32 range]."""
+    out = (C.c_ulonglong * 4)()
+    _ck(lib().des_gpu_softf64_check(device, n, seed, out), "des_gpu_softf64_check")
+    return list(out)
 
 
 def pin(state):

@@ -479,6 +479,14 @@ const char *des_gpu_error_string(int code);
 long long   des_gpu_device_bytes(const des_gpu *g);
 /* number of kernels one des_gpu_step launches per step */
 int         des_gpu_kernels_per_step(const des_gpu *g);
+/* Self-check of the integer-pipe FP64 multiply and FP64 -> FP32 conversion
+ * that the step kernels use in place of FP64 unit instructions (no reference
+ * counterpart): n seeded pseudo-random operands per kind on `device`,
+ * compared bit for bit with the device's own FP64 instructions.
+ * mismatches[0..3]: multiply on any bit patterns, multiply on operands near
+ * 1, conversion on any bit patterns, conversion within the FP32 range. */
+int         des_gpu_softf64_check(int device, long long n, unsigned long long seed,
+                                  unsigned long long mismatches[4]);
 
 #ifdef __cplusplus
 }
