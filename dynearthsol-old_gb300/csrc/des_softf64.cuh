@@ -144,21 +144,59 @@ uint64_t mul_slow(uint64_t a, uint64_t b)
     return round_pack(sign, e, r);
 }
 
-// x * y as the FP64 unit rounds it.  Fast path: both significands shifted
-// to bit 63; the top 64 bits of their 128-bit product carry the result and
-// the low 64 bits only a sticky bit, which rounds like the exact product
-// because the rounding position is 11 bits above it.
+// 32x32 -> 64 products with a 64-bit addend; on the device as PTX
+// mul.wide.u32 / mad.wide.u32 instructions, which the compiler's IR passes
+// keep as they are
+DES_SF_HD uint64_t wide_mul(uint32_t x, uint32_t y)
+{
+#if defined(__CUDA_ARCH__)
+    uint64_t r;
+    asm("mul.wide.u32 %0, %1, %2;" : "=l"(r) : "r"(x), "r"(y));
+    return r;
+#else
+    return (uint64_t)x * y;
+#endif
+}
+
+DES_SF_HD uint64_t wide_mad(uint32_t x, uint32_t y, uint64_t c)
+{
+#if defined(__CUDA_ARCH__)
+    uint64_t r;
+    asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(r) : "r"(x), "r"(y), "l"(c));
+    return r;
+#else
+    return (uint64_t)x * y + c;
+#endif
+}
+
+// x * y as the FP64 unit rounds it.  Fast path (normal operands, normal
+// result) in 32-bit pieces: with the significands A = a1 2^32 + a0 and
+// B = b1 2^32 + b0 (a1, b1 of 21 bits), four 32x32 -> 64 products give the
+// 106-bit P = A B as p11 2^64 + mid 2^32 + low.  The significand of the
+// result is P >> (52 + t), t = 1 when P >= 2^105; the bits below it decide
+// the rounding (round bit, then a sticky OR of the rest).
 DES_SF_HD double mul(double x, double y)
 {
     const uint64_t a = bits(x), b = bits(y);
-    const uint32_t ea = (uint32_t)(a >> 52) & 0x7ff, eb = (uint32_t)(b >> 52) & 0x7ff;
+    const uint32_t ah = (uint32_t)(a >> 32), bh = (uint32_t)(b >> 32);
+    const uint32_t ea = (ah >> 20) & 0x7ff, eb = (bh >> 20) & 0x7ff;
     if (ea - 1 < 2046u && eb - 1 < 2046u) {
-        const uint64_t fa = ((a & kFrac) | kHidden) << 11, fb = ((b & kFrac) | kHidden) << 11;
-        const uint64_t hi = mulhi64(fa, fb), lo = fa * fb;
-        const int lz = (int)(1 - (hi >> 63));
-        const int e = (int)(ea + eb) - 1022 - lz;
-        if ((uint32_t)(e - 1) < 2046u)
-            return from_bits(round_pack((a ^ b) & kSign, e, (hi << lz) | (uint64_t)(lo != 0)));
+        const uint32_t a0 = (uint32_t)a, b0 = (uint32_t)b;
+        const uint32_t a1 = (ah & 0xfffffu) | 0x100000u, b1 = (bh & 0xfffffu) | 0x100000u;
+        const uint64_t p00 = wide_mul(a0, b0);
+        const uint64_t p01 = wide_mad(a0, b1, p00 >> 32);
+        const uint64_t p10 = wide_mad(a1, b0, p01);
+        const uint64_t p11 = wide_mad(a1, b1, p10 >> 32);
+        const uint32_t mid = (uint32_t)p10, low = (uint32_t)p00;
+        const uint32_t t = (uint32_t)(p11 >> 41);
+        const int e = (int)(ea + eb) - 1023 + (int)t;
+        if ((uint32_t)(e - 1) < 2046u) {
+            const uint32_t sh = 12 - t;
+            const uint64_t m = (p11 << sh) | (mid >> (32 - sh));
+            const uint32_t rem = mid << sh;
+            const uint32_t up = (rem >> 31) & (uint32_t)((((rem << 1) | low) != 0) | ((uint32_t)m & 1));
+            return from_bits(((((uint64_t)(e - 1)) << 52) + m + up) | ((a ^ b) & kSign));
+        }
     }
     // a zero times a finite number (frequent: zero velocity components and
     // shape-function derivatives) without the call
