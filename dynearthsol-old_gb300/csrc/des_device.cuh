@@ -404,13 +404,19 @@ __device__ __forceinline__ int principal3(const double *s, double p[3], double v
 
 // ---- rheology (rheology.cxx:108-302, 3D) ----------------------------------
 
+// a product as the FP64 unit rounds it, on the integer pipes for FP64
+// (sf::mul); FP32 products stay on the FP32 pipe
+__device__ __forceinline__ double pmul(double a, double b) { return sf::mul(a, b); }
+__device__ __forceinline__ float pmul(float a, float b) { return a * b; }
+
 template <class R>
 __device__ __forceinline__ void elastic(R bulkm, R shearm, const R *de, R *s)
 {
     R lambda = bulkm - R(2.) / R(3) * shearm;
     R dev = tr3(de);
-    for (int i = 0; i < 3; ++i) s[i] += 2 * shearm * de[i] + lambda * dev;
-    for (int i = 3; i < 6; ++i) s[i] += 2 * shearm * de[i];
+    const R g2 = 2 * shearm;
+    for (int i = 0; i < 3; ++i) s[i] += pmul(g2, de[i]) + pmul(lambda, dev);
+    for (int i = 3; i < 6; ++i) s[i] += pmul(g2, de[i]);
 }
 
 template <class R>

@@ -193,9 +193,10 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
         double div = tr3(edot);
         for (int i = 0; i < 3; ++i) edot[i] += (edv - div) / 3;
     }
-    for (int i = 0; i < 6; ++i) es[i] += edot[i] * dt;
+    // (products on the integer pipes, sf::mul)
     double de[6];
-    for (int i = 0; i < 6; ++i) de[i] = edot[i] * dt;
+    for (int i = 0; i < 6; ++i) de[i] = sf::mul(edot[i], dt);
+    for (int i = 0; i < 6; ++i) es[i] += de[i];
     int flags = 0;
     switch (K.rheol) {
     case 1:   // elastic
@@ -633,10 +634,13 @@ __device__ __forceinline__ void force_elem_body(const Dev &d, int e, int4 c, con
         load_nodal4(d.T, c, Tn);
         buoy = mat_rho(K.M, K.M.mix[d.mix[e]], elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3])) * K.gravity / 4;
     }
+    // (products on the integer pipes, sf::mul)
     for (int i = 0; i < 4; ++i) {
-        d.tmp[(i)*E + e] = (s[0] * dx[i] + s[3] * dy[i] + s[4] * dz[i]) * vol;
-        d.tmp[(i + 4) * E + e] = (s[3] * dx[i] + s[1] * dy[i] + s[5] * dz[i]) * vol;
-        d.tmp[(i + 8) * E + e] = (s[4] * dx[i] + s[5] * dy[i] + s[2] * dz[i] + buoy) * vol;
+        d.tmp[(i)*E + e] = sf::mul(sf::mul(s[0], dx[i]) + sf::mul(s[3], dy[i]) + sf::mul(s[4], dz[i]), vol);
+        d.tmp[(i + 4) * E + e] =
+            sf::mul(sf::mul(s[3], dx[i]) + sf::mul(s[1], dy[i]) + sf::mul(s[5], dz[i]), vol);
+        d.tmp[(i + 8) * E + e] =
+            sf::mul(sf::mul(s[4], dx[i]) + sf::mul(s[5], dy[i]) + sf::mul(s[2], dz[i]) + buoy, vol);
     }
 }
 __global__ void k_force_elem(Dev d)
