@@ -218,11 +218,11 @@ __device__ __forceinline__ void list_append(unsigned *count, int *list, bool tak
     if (take) list[base + __popc(m & ((1u << lane) - 1u))] = e;
 }
 
-// E-B1
+// E-B1, over the elements from e0 (a multiple of the block size)
 template <int RHEOL>
-__global__ void kf_fe_b_ep(DevF d)
+__global__ void kf_fe_b_ep(DevF d, int e0)
 {
-    const int e = gtid();
+    const int e = e0 + gtid();
     if (e == 0) d.clk->mass_valid = 1;
     const bool live = e < d.nelem;
     bool pending = false;

@@ -21,6 +21,7 @@ const int kElemBlock = 128;
 const int kNodeBlock = 256;
 const int kStepKernels = 6;
 const int kEaChunks = 8;   // E-A launches of the host-buffer step (downloads overlap them)
+const int kEbChunks = 8;   // E-B launches of the host-buffer step (its inputs come up chunk by chunk)
 
 inline int blocks(long long n, int b) { return (int)((n + b - 1) / b); }
 
@@ -63,6 +64,11 @@ struct des_gpu {
     long long dl_elems = 0;
     cudaEvent_t head_done = nullptr;      // a step's passes before E-A are done
     cudaEvent_t up_done = nullptr;        // the copy stream's uploads are done
+    // host-to-device copies of the host-buffer step, on their own stream so
+    // that they run beside the device-to-host copies of the copy stream;
+    // one event per element chunk
+    cudaStream_t up_stream = nullptr;
+    cudaEvent_t up_chunk[kEbChunks] = {};
     cudaEvent_t snap_ready = nullptr, snap_done = nullptr;
     int avg_interval = 0;                 // Output::average_fields every step when > 0
     double *avg_c0 = nullptr, *avg_strain0 = nullptr, *avg_stress = nullptr, *avg_dpls = nullptr,
@@ -515,33 +521,57 @@ void launch_surface(des_gpu *g)
     k_surface_nodes<<<blocks(g->nnode, kNodeBlock), kNodeBlock, 0, g->stream>>>(g->d);
 }
 
+// the first kernel of pass E-B over the element blocks [b0, b1)
+void launch_eb_first(des_gpu *g, int b0, int b1)
+{
+    cudaStream_t st = g->stream;
+    const int n = b1 - b0, e0 = b0 * kElemBlock;
+    if (g->prec == DES_PREC_FP32) {
+        if (g->hF.rheol == 7)
+            kf_fe_b_ep<7><<<n, kElemBlock, 0, st>>>(g->f, e0);
+        else if (g->hF.rheol == 5)
+            kf_fe_b_ep<5><<<n, kElemBlock, 0, st>>>(g->f, e0);
+        else
+            kf_fe_b<<<n, kElemBlock, 0, st>>>(g->f, e0);
+    } else if (g->d.ret_log) {
+        k_fe_b_t<true><<<n, kElemBlock, 0, st>>>(g->d, e0);
+    } else {
+        k_fe_b_t<false><<<n, kElemBlock, 0, st>>>(g->d, e0);
+    }
+}
+
+// the rest of pass E-B once its first kernel has covered every element: in
+// the FP32 form with rh_ep / rh_evp, the network (with a closure) and the
+// exact return map, each over the dense list the first kernel left
+void launch_eb_rest(des_gpu *g)
+{
+    if (g->prec != DES_PREC_FP32 || (g->hF.rheol != 5 && g->hF.rheol != 7)) return;
+    cudaStream_t st = g->stream;
+    const DevF &f = g->f;
+    const int nn_grid = 4 * g->sms, exact_grid = 8 * g->sms;
+    if (g->hF.rheol == 7) {
+        if (g->closure) kf_nn_list<7><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
+        kf_exact_list<7><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
+    } else {
+        if (g->closure) kf_nn_list<5><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
+        kf_exact_list<5><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
+    }
+}
+
 // pass k of N-A, E-B, N-B, E-C, N-C (0..4) of one step
 void launch_pass(des_gpu *g, int k)
 {
     const int nb = blocks(g->nnode, kNodeBlock), eb = blocks(g->nelem, kElemBlock);
     cudaStream_t st = g->stream;
+    if (k == 1) {
+        launch_eb_first(g, 0, eb);
+        launch_eb_rest(g);
+        return;
+    }
     if (g->prec == DES_PREC_FP32) {
         const DevF &f = g->f;
         switch (k) {
         case 0: kf_fn_a<<<nb, kNodeBlock, 0, st>>>(f); break;
-        case 1:
-            if (g->hF.rheol == 5 || g->hF.rheol == 7) {
-                // elastic elements, then the network (with a closure), then
-                // the exact return map, each over a dense list
-                const int nn_grid = 4 * g->sms, exact_grid = 8 * g->sms;
-                if (g->hF.rheol == 7) {
-                    kf_fe_b_ep<7><<<eb, kElemBlock, 0, st>>>(f);
-                    if (g->closure) kf_nn_list<7><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
-                    kf_exact_list<7><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
-                } else {
-                    kf_fe_b_ep<5><<<eb, kElemBlock, 0, st>>>(f);
-                    if (g->closure) kf_nn_list<5><<<nn_grid, kNnListBlock, sizeof(NnListSmem), st>>>(f, g->dnet);
-                    kf_exact_list<5><<<exact_grid, 128, 0, st>>>(f, g->closure ? 0 : 1);
-                }
-            } else {
-                kf_fe_b<<<eb, kElemBlock, 0, st>>>(f);
-            }
-            break;
         case 2: kf_sg_gather<<<nb, kNodeBlock, 0, st>>>(f); break;
         case 3: kf_fe_c<<<eb, kElemBlock, 0, st>>>(f); break;
         default:
@@ -555,12 +585,6 @@ void launch_pass(des_gpu *g, int k)
         const Dev &d = g->d;
         switch (k) {
         case 0: k_fn_a<<<nb, kNodeBlock, 0, st>>>(d); break;
-        case 1:
-            if (d.ret_log)
-                k_fe_b_t<true><<<eb, kElemBlock, 0, st>>>(d);
-            else
-                k_fe_b_t<false><<<eb, kElemBlock, 0, st>>>(d);
-            break;
         case 2: k_sg_gather<<<nb, kNodeBlock, 0, st>>>(d); break;
         case 3: k_fe_c<<<eb, kElemBlock, 0, st>>>(d); break;
         default:
@@ -650,6 +674,9 @@ int ensure_copy_stream(des_gpu *g)
     if (!g->copy_stream) DES_CUDA(cudaStreamCreateWithFlags(&g->copy_stream, cudaStreamNonBlocking));
     if (!g->head_done) DES_CUDA(cudaEventCreateWithFlags(&g->head_done, cudaEventDisableTiming));
     if (!g->up_done) DES_CUDA(cudaEventCreateWithFlags(&g->up_done, cudaEventDisableTiming));
+    if (!g->up_stream) DES_CUDA(cudaStreamCreateWithFlags(&g->up_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : g->up_chunk)
+        if (!e) DES_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     return DES_OK;
 }
 
@@ -956,6 +983,12 @@ int des_gpu_destroy(des_gpu *g)
         cudaStreamSynchronize(g->copy_stream);
         cudaStreamDestroy(g->copy_stream);
     }
+    if (g->up_stream) {
+        cudaStreamSynchronize(g->up_stream);
+        cudaStreamDestroy(g->up_stream);
+    }
+    for (cudaEvent_t e : g->up_chunk)
+        if (e) cudaEventDestroy(e);
     if (g->snap_ready) cudaEventDestroy(g->snap_ready);
     if (g->head_done) cudaEventDestroy(g->head_done);
     if (g->up_done) cudaEventDestroy(g->up_done);
@@ -1781,59 +1814,17 @@ static int derive_geometry(des_gpu *g)
     return finish(g);
 }
 
-int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
-                      des_step_report *report)
+// the end of a host-buffer step once passes N-A .. N-C are queued and their
+// fields are on their way down (the download buffer filled up to off): E-A in
+// element chunks, each chunk's rows of the element fields going to the host
+// while the next chunk computes, then the averaging, the clock, the nodal
+// masses and the late nodal fields
+static int step_host_tail(des_gpu *g, des_state_view *host, unsigned mask, const std::vector<DownPart> &late,
+                          long long off, des_step_report *report)
 {
-    if (!g || !host || nsteps < 0) return DES_ERR_ARG;
-    unsigned up = mask & ~kStepOutputs;
-    // with coordinates and temperature in hand, volume, shape derivatives and
-    // masses are recomputed on the device rather than copied (1.0 GB fewer
-    // host-to-device bytes per step for 9.6M elements); volume_old is copied
-    const unsigned derived = DES_F_VOLUME | DES_F_SHAPE | DES_F_MASS;
-    const bool derive = (up & DES_F_COORD) && (up & DES_F_TEMPERATURE) && (up & derived) == derived;
-    if (derive) up &= ~derived;
-    // while the geometry is derived, the element fields it does not read come
-    // over the copy engine on the second stream (the FP32 form's derivation
-    // reads the reference stress, so its stress is uploaded first)
-    unsigned later = 0;
-    if (derive) later = up & (DES_F_STRAIN | DES_F_PLSTRAIN | (g->prec == DES_PREC_FP64 ? DES_F_STRESS : 0u));
-    int rc = des_gpu_upload(g, host, up & ~later);
-    if (rc) return rc;
-    if (derive) {
-        if (host->nelem != g->nelem || !host->volume_old) return DES_ERR_ARG;
-        std::vector<DownPart> all;
-        if ((rc = down_parts(g, host, mask, all))) return rc;
-        long long down = 0;
-        for (const DownPart &q : all) down += q.ncomp * q.rows;
-        if ((rc = upload_elements_async(g, host, later, down))) return rc;
-        if ((rc = derive_geometry(g))) return rc;
-        if ((rc = finish_elements_async(g, host, later))) return rc;
-    }
-    if (nsteps == 0) return des_gpu_download(g, host, mask);
-    // every step but the last as the graph; the last as its passes, so that
-    // the fields finished before E-A download on the copy stream while E-A
-    // runs (the host link is the bound of this entry point)
-    if (nsteps > 1 && (rc = des_gpu_step(g, nsteps - 1, nullptr))) return rc;
-    if ((rc = prime(g))) return rc;
-    std::vector<DownPart> all, late;
-    if ((rc = down_parts(g, host, mask, all)) || (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)))
-        return rc;
-    long long need = 0;
-    for (const DownPart &q : all) need += q.ncomp * q.rows;
-    if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, need))) return rc;
+    int rc = DES_OK;
     std::vector<DownPart> late_elem, late_node;
     for (const DownPart &q : late) (q.elem ? late_elem : late_node).push_back(q);
-    long long off = 0;
-    // each field downloads after the pass that finishes it
-    for (int k = 0; k < 5 && !rc; ++k) {
-        launch_pass(g, k);
-        rc = cuda_rc(cudaGetLastError());
-        std::vector<DownPart> done;
-        if (!rc) rc = down_parts(g, host, mask & kFinishedAfterPass[k], done);
-        if (!rc) rc = download_async(g, done, &off);
-    }
-    // E-A in element chunks; each chunk's rows of the element fields go to
-    // the host while the next chunk computes
     const int nb = blocks(g->nelem, kElemBlock), nchunk = std::min(kEaChunks, nb);
     std::vector<long long> base(late_elem.size());
     for (size_t i = 0; i < late_elem.size(); ++i) {
@@ -1869,6 +1860,158 @@ int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nstep
         host->steps = c.steps;
     }
     return finish(g);
+}
+
+// One step from host buffers with the element fields E-B reads (`later`)
+// coming up chunk by chunk on the upload stream while the geometry is
+// derived and N-A runs: E-B runs on each chunk as it lands, and in the FP64
+// form the fields E-B finishes go down chunk by chunk on the copy stream
+// while later chunks still come up, so the two directions of the host link
+// run at once.  (The FP32 form's list kernels follow the last chunk, so its
+// E-B fields go down whole.)
+static int step_host_pipelined(des_gpu *g, des_state_view *host, unsigned mask, unsigned later,
+                               des_step_report *report)
+{
+    const long long E = g->nelem;
+    int rc;
+    const std::vector<UpPart> ups = up_parts(g, host, later);
+    long long U = 0;
+    for (const UpPart &q : ups) {
+        if (!q.host) return DES_ERR_ARG;
+        U += q.ncomp * E;
+    }
+    std::vector<DownPart> all, late, eb;
+    if ((rc = down_parts(g, host, mask, all)) || (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)) ||
+        (rc = down_parts(g, host, mask & kFinishedAfterPass[1], eb)))
+        return rc;
+    long long D = 0;
+    for (const DownPart &q : all) D += q.ncomp * q.rows;
+    if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, U + D))) return rc;
+    // the buffer's previous contents have left
+    DES_CUDA(cudaStreamSynchronize(g->copy_stream));
+    DES_CUDA(cudaStreamSynchronize(g->up_stream));
+    const int nb = blocks(E, kElemBlock), nchunk = std::min(kEbChunks, nb);
+    auto chunk_block = [&](int k) { return (int)((long long)nb * k / nchunk); };
+    auto block_row = [&](int b) { return std::min<long long>((long long)b * kElemBlock, E); };
+    // uploads into the buffer's first U doubles: each part's host rows at the
+    // part's place, chunk by chunk, one event per chunk
+    for (int k = 0; k < nchunk; ++k) {
+        const long long r0 = block_row(chunk_block(k)), r1 = block_row(chunk_block(k + 1));
+        long long uoff = 0;
+        for (const UpPart &q : ups) {
+            DES_CUDA(cudaMemcpyAsync(g->dl + uoff + r0 * q.ncomp, q.host + r0 * q.ncomp,
+                                     sizeof(double) * q.ncomp * (r1 - r0), cudaMemcpyHostToDevice,
+                                     g->up_stream));
+            uoff += q.ncomp * E;
+        }
+        DES_CUDA(cudaEventRecord(g->up_chunk[k], g->up_stream));
+    }
+    // volume, shape derivatives and masses from the coordinates, the
+    // next-step contributions (neither reads the `later` fields), N-A
+    if ((rc = derive_geometry(g)) || (rc = prime(g))) return rc;
+    long long off = U;
+    launch_pass(g, 0);
+    if ((rc = cuda_rc(cudaGetLastError()))) return rc;
+    {
+        std::vector<DownPart> done;
+        if ((rc = down_parts(g, host, mask & kFinishedAfterPass[0], done)) || (rc = download_async(g, done, &off)))
+            return rc;
+    }
+    // E-B chunk by chunk as its inputs land
+    std::vector<long long> ebase(eb.size());
+    for (size_t i = 0; i < eb.size(); ++i) {
+        ebase[i] = off;
+        off += eb[i].ncomp * eb[i].rows;
+    }
+    const bool per_chunk = g->prec == DES_PREC_FP64;
+    for (int k = 0; k < nchunk && !rc; ++k) {
+        const int b0 = chunk_block(k), b1 = chunk_block(k + 1);
+        const long long r0 = block_row(b0), nr = block_row(b1) - r0;
+        DES_CUDA(cudaStreamWaitEvent(g->stream, g->up_chunk[k], 0));
+        long long uoff = 0;
+        for (const UpPart &q : ups) {
+            const double *src = g->dl + uoff + r0 * q.ncomp;
+            if (q.dst64)
+                k_aos_to_soa<<<blocks(nr * q.ncomp, 256), 256, 0, g->stream>>>(src, q.dst64, q.ncomp, nr, r0, E);
+            else
+                k_aos_to_soa_f<<<blocks(nr * q.ncomp, 256), 256, 0, g->stream>>>(src, q.dst32, q.ncomp, nr, r0, E);
+            uoff += q.ncomp * E;
+        }
+        launch_eb_first(g, b0, b1);
+        rc = cuda_rc(cudaGetLastError());
+        if (per_chunk)
+            for (size_t i = 0; i < eb.size() && !rc; ++i) rc = download_rows_async(g, eb[i], ebase[i], r0, nr);
+    }
+    if (rc) return rc;
+    launch_eb_rest(g);
+    if ((rc = cuda_rc(cudaGetLastError()))) return rc;
+    if (!per_chunk)
+        for (size_t i = 0; i < eb.size() && !rc; ++i) rc = download_rows_async(g, eb[i], ebase[i], 0, eb[i].rows);
+    // N-B, E-C, N-C, each field going down after the pass that finishes it
+    for (int k = 2; k < 5 && !rc; ++k) {
+        launch_pass(g, k);
+        rc = cuda_rc(cudaGetLastError());
+        std::vector<DownPart> done;
+        if (!rc) rc = down_parts(g, host, mask & kFinishedAfterPass[k], done);
+        if (!rc) rc = download_async(g, done, &off);
+    }
+    if (rc) return rc;
+    return step_host_tail(g, host, mask, late, off, report);
+}
+
+int des_gpu_step_host(des_gpu *g, des_state_view *host, unsigned mask, int nsteps,
+                      des_step_report *report)
+{
+    if (!g || !host || nsteps < 0) return DES_ERR_ARG;
+    unsigned up = mask & ~kStepOutputs;
+    // with coordinates and temperature in hand, volume, shape derivatives and
+    // masses are recomputed on the device rather than copied (1.0 GB fewer
+    // host-to-device bytes per step for 9.6M elements); volume_old is copied
+    const unsigned derived = DES_F_VOLUME | DES_F_SHAPE | DES_F_MASS;
+    const bool derive = (up & DES_F_COORD) && (up & DES_F_TEMPERATURE) && (up & derived) == derived;
+    if (derive) up &= ~derived;
+    // while the geometry is derived, the element fields it does not read come
+    // over the copy engine on a second stream (the FP32 form's derivation
+    // reads the reference stress, so its stress is uploaded first)
+    unsigned later = 0;
+    if (derive) later = up & (DES_F_STRAIN | DES_F_PLSTRAIN | (g->prec == DES_PREC_FP64 ? DES_F_STRESS : 0u));
+    int rc = des_gpu_upload(g, host, up & ~later);
+    if (rc) return rc;
+    if (derive && host->nelem == g->nelem && host->volume_old && nsteps == 1)
+        return step_host_pipelined(g, host, mask, later, report);
+    if (derive) {
+        if (host->nelem != g->nelem || !host->volume_old) return DES_ERR_ARG;
+        std::vector<DownPart> all;
+        if ((rc = down_parts(g, host, mask, all))) return rc;
+        long long down = 0;
+        for (const DownPart &q : all) down += q.ncomp * q.rows;
+        if ((rc = upload_elements_async(g, host, later, down))) return rc;
+        if ((rc = derive_geometry(g))) return rc;
+        if ((rc = finish_elements_async(g, host, later))) return rc;
+    }
+    if (nsteps == 0) return des_gpu_download(g, host, mask);
+    // every step but the last as the graph; the last as its passes, so that
+    // the fields finished before E-A download on the copy stream while E-A
+    // runs (the host link is the bound of this entry point)
+    if (nsteps > 1 && (rc = des_gpu_step(g, nsteps - 1, nullptr))) return rc;
+    if ((rc = prime(g))) return rc;
+    std::vector<DownPart> all, late;
+    if ((rc = down_parts(g, host, mask, all)) || (rc = down_parts(g, host, mask & ~kBeforeLastPass, late)))
+        return rc;
+    long long need = 0;
+    for (const DownPart &q : all) need += q.ncomp * q.rows;
+    if ((rc = ensure_copy_stream(g)) || (rc = ensure_download_buffer(g, need))) return rc;
+    long long off = 0;
+    // each field downloads after the pass that finishes it
+    for (int k = 0; k < 5 && !rc; ++k) {
+        launch_pass(g, k);
+        rc = cuda_rc(cudaGetLastError());
+        std::vector<DownPart> done;
+        if (!rc) rc = down_parts(g, host, mask & kFinishedAfterPass[k], done);
+        if (!rc) rc = download_async(g, done, &off);
+    }
+    if (rc) return rc;
+    return step_host_tail(g, host, mask, late, off, report);
 }
 
 // remesh (remeshing.cxx:1963-2067) after the host's new mesh, interpolation

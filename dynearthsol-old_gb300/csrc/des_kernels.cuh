@@ -1066,10 +1066,11 @@ constexpr int kRetRecord = 24;
 // increment, [21] element index (int bits), [22] step (int bits), [23] the
 // dilation factor anpsi of the return
 
+// (over the elements from e0, a multiple of the block size)
 template <bool LOG>
-__global__ void k_fe_b_t(Dev d)
+__global__ void k_fe_b_t(Dev d, int e0)
 {
-    int e = gtid();
+    int e = e0 + gtid();
     if (e == 0) d.clk->mass_valid = 1;
     bool live = e < d.nelem;
     int flags = 0;

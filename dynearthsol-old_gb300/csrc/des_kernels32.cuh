@@ -449,10 +449,11 @@ __global__ void kf_fn_a(DevF d)
     d.ntmp[n] = dv / vn;
 }
 
-// E-B: edvoldt + update_stress (FP32 with the FP64 return map where needed)
-__global__ void kf_fe_b(DevF d)
+// E-B: edvoldt + update_stress (FP32 with the FP64 return map where needed),
+// over the elements from e0 (a multiple of the block size)
+__global__ void kf_fe_b(DevF d, int e0)
 {
-    int e = gtid();
+    int e = e0 + gtid();
     if (e == 0) d.clk->mass_valid = 1;
     bool live = e < d.nelem;
     int flags = 0;
