@@ -691,18 +691,17 @@ __device__ __forceinline__ void spin_and_rate(const double V[4][3], const double
                                               const double *dz, double &w3, double &w4, double &w5,
                                               double D[6])
 {
-    // the products on the integer pipes (sf::mul rounds as the FP64 unit does)
     D[0] = 0;
-    for (int i = 0; i < 4; ++i) D[0] += sf::mul(V[i][0], dx[i]);
+    for (int i = 0; i < 4; ++i) D[0] += V[i][0] * dx[i];
     D[1] = 0;
-    for (int i = 0; i < 4; ++i) D[1] += sf::mul(V[i][1], dy[i]);
+    for (int i = 0; i < 4; ++i) D[1] += V[i][1] * dy[i];
     D[2] = 0;
-    for (int i = 0; i < 4; ++i) D[2] += sf::mul(V[i][2], dz[i]);
+    for (int i = 0; i < 4; ++i) D[2] += V[i][2] * dz[i];
     double t3 = 0, t4 = 0, t5 = 0, u3 = 0, u4 = 0, u5 = 0;
     for (int i = 0; i < 4; ++i) {
-        const double xy = sf::mul(V[i][0], dy[i]), yx = sf::mul(V[i][1], dx[i]);
-        const double xz = sf::mul(V[i][0], dz[i]), zx = sf::mul(V[i][2], dx[i]);
-        const double yz = sf::mul(V[i][1], dz[i]), zy = sf::mul(V[i][2], dy[i]);
+        const double xy = V[i][0] * dy[i], yx = V[i][1] * dx[i];
+        const double xz = V[i][0] * dz[i], zx = V[i][2] * dx[i];
+        const double yz = V[i][1] * dz[i], zy = V[i][2] * dy[i];
         t3 += xy + yx;
         u3 += xy - yx;
         t4 += xz + zx;
