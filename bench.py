@@ -526,7 +526,7 @@ def run_ours(args):
     # exactly rounded integer-pipe products (sf::mul) instead, which is what
     # lets the step beat this pipe's bound for the reference's arithmetic
     # (604 FP64 instructions per element-step when every product is on it).
-    fp64_ops = {"N-A": 23.1, "E-B": 57.0, "N-B": 5.4, "E-C": 57.1, "N-C": 19.7, "E-A": 257.3}
+    fp64_ops = {"N-A": 23.1, "E-B": 57.0, "N-B": 5.4, "E-C": 57.1, "N-C": 19.7, "E-A": 293.0}
     fp64_ops_all_on_pipe = 604.2
     import torch
     sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -592,10 +592,10 @@ def run_ours(args):
         "gpu_launches": dev.kernels_per_step * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
-                     # DRAM bytes per launch: 510 B/element read + written by E-A in an ncu
+                     # DRAM bytes per launch: 463 B/element read + written by E-A in an ncu
                      # capture on a 100x100x40 box (traffic grows with the element count),
                      # scaled to this launch
-                     "traffic": 510.0 * mesh.nelem if names[top] == "E-A" else None,
+                     "traffic": 463.0 * mesh.nelem if names[top] == "E-A" else None,
                      "peak_kind": hbm_kind,
                      "step_alg_bytes_per_elem": B_ELEM + B_NODE * r,
                      "step_achieved_gbs": step_gbs, "step_frac": step_gbs / hbm,
