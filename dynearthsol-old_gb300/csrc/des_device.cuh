@@ -217,26 +217,29 @@ __device__ __forceinline__ void plastic_props(const MatTable &M, const Mix &x, d
 
 __device__ __forceinline__ double sq(double x) { return x * x; }
 
+// (the products on the integer pipes, sf::mul, rounded as the FP64 unit
+// rounds them; the square roots, atan2 and sincos on the FP64 unit)
 __device__ __forceinline__ void eig_cardano(const double *A, double w[3])
 {
+    using sf::mul;
     const double a00 = A[0], a11 = A[1], a22 = A[2], a01 = A[3], a02 = A[4], a12 = A[5];
-    double de = a01 * a12;
-    double dd = sq(a01);
-    double ee = sq(a12);
-    double ff = sq(a02);
+    double de = mul(a01, a12);
+    double dd = mul(a01, a01);
+    double ee = mul(a12, a12);
+    double ff = mul(a02, a02);
     double m = a00 + a11 + a22;
-    double c1 = (a00 * a11 + a00 * a22 + a11 * a22) - (dd + ee + ff);
-    double c0 = a22 * dd + a00 * ee + a11 * ff - a00 * a11 * a22 - 2.0 * a02 * de;
-    double p = sq(m) - 3.0 * c1;
-    double q = m * (p - (3.0 / 2.0) * c1) - (27.0 / 2.0) * c0;
+    double c1 = (mul(a00, a11) + mul(a00, a22) + mul(a11, a22)) - (dd + ee + ff);
+    double c0 = mul(a22, dd) + mul(a00, ee) + mul(a11, ff) - mul(mul(a00, a11), a22) - mul(mul(2.0, a02), de);
+    double p = mul(m, m) - mul(3.0, c1);
+    double q = mul(m, p - mul(3.0 / 2.0, c1)) - mul(27.0 / 2.0, c0);
     double sqrt_p = sqrt(fabs(p));
-    double phi = 27.0 * (0.25 * sq(c1) * (p - c1) + c0 * (q + 27.0 / 4.0 * c0));
-    phi = (1.0 / 3.0) * atan2(sqrt(fabs(phi)), q);
+    double phi = mul(27.0, mul(mul(0.25, mul(c1, c1)), p - c1) + mul(c0, q + mul(27.0 / 4.0, c0)));
+    phi = mul(1.0 / 3.0, atan2(sqrt(fabs(phi)), q));
     double sp, cp;
     sincos(phi, &sp, &cp);
-    double c = sqrt_p * cp;
-    double s = (1.0 / 1.73205080756887729352744634151) * sqrt_p * sp;
-    w[1] = (1.0 / 3.0) * (m - c);
+    double c = mul(sqrt_p, cp);
+    double s = mul(mul(1.0 / 1.73205080756887729352744634151, sqrt_p), sp);
+    w[1] = mul(1.0 / 3.0, m - c);
     w[2] = w[1] + s;
     w[0] = w[1] + c;
     w[1] -= s;
@@ -348,6 +351,7 @@ __device__ __forceinline__ int eig_hybrid(const double *A, double Q[3][3], doubl
 {
     const double a00 = A[0], a11 = A[1], a01 = A[3], a02 = A[4], a12 = A[5];
     double norm, error, t, u;
+    using sf::mul;
     eig_cardano(A, w);
     t = fabs(w[0]);
     if ((u = fabs(w[1])) > t) t = u;
@@ -355,28 +359,28 @@ __device__ __forceinline__ int eig_hybrid(const double *A, double Q[3][3], doubl
     if (t < 1.0)
         u = t;
     else
-        u = sq(t);
-    error = 256.0 * kEps * sq(u);
-    double q01 = a01 * a12 - a02 * a11;
-    double q11 = a02 * a01 - a12 * a00;
-    double q21 = sq(a01);
-    Q[0][0] = q01 + a02 * w[0];
-    Q[1][0] = q11 + a12 * w[0];
-    Q[2][0] = (a00 - w[0]) * (a11 - w[0]) - q21;
-    norm = sq(Q[0][0]) + sq(Q[1][0]) + sq(Q[2][0]);
+        u = mul(t, t);
+    error = mul(mul(256.0, kEps), mul(u, u));
+    double q01 = mul(a01, a12) - mul(a02, a11);
+    double q11 = mul(a02, a01) - mul(a12, a00);
+    double q21 = mul(a01, a01);
+    Q[0][0] = q01 + mul(a02, w[0]);
+    Q[1][0] = q11 + mul(a12, w[0]);
+    Q[2][0] = mul(a00 - w[0], a11 - w[0]) - q21;
+    norm = mul(Q[0][0], Q[0][0]) + mul(Q[1][0], Q[1][0]) + mul(Q[2][0], Q[2][0]);
     if (norm <= error) return eig_ql(A, Q, w) == 0 ? 1 : -1;
     norm = sqrt(1.0 / norm);
-    for (int j = 0; j < 3; j++) Q[j][0] = Q[j][0] * norm;
-    Q[0][1] = q01 + a02 * w[1];
-    Q[1][1] = q11 + a12 * w[1];
-    Q[2][1] = (a00 - w[1]) * (a11 - w[1]) - q21;
-    norm = sq(Q[0][1]) + sq(Q[1][1]) + sq(Q[2][1]);
+    for (int j = 0; j < 3; j++) Q[j][0] = mul(Q[j][0], norm);
+    Q[0][1] = q01 + mul(a02, w[1]);
+    Q[1][1] = q11 + mul(a12, w[1]);
+    Q[2][1] = mul(a00 - w[1], a11 - w[1]) - q21;
+    norm = mul(Q[0][1], Q[0][1]) + mul(Q[1][1], Q[1][1]) + mul(Q[2][1], Q[2][1]);
     if (norm <= error) return eig_ql(A, Q, w) == 0 ? 1 : -1;
     norm = sqrt(1.0 / norm);
-    for (int j = 0; j < 3; j++) Q[j][1] = Q[j][1] * norm;
-    Q[0][2] = Q[1][0] * Q[2][1] - Q[2][0] * Q[1][1];
-    Q[1][2] = Q[2][0] * Q[0][1] - Q[0][0] * Q[2][1];
-    Q[2][2] = Q[0][0] * Q[1][1] - Q[1][0] * Q[0][1];
+    for (int j = 0; j < 3; j++) Q[j][1] = mul(Q[j][1], norm);
+    Q[0][2] = mul(Q[1][0], Q[2][1]) - mul(Q[2][0], Q[1][1]);
+    Q[1][2] = mul(Q[2][0], Q[0][1]) - mul(Q[0][0], Q[2][1]);
+    Q[2][2] = mul(Q[0][0], Q[1][1]) - mul(Q[1][0], Q[0][1]);
     return 0;
 }
 
@@ -557,14 +561,16 @@ __device__ __forceinline__ int plastic_return(double bulkm, double shearm, doubl
         p[2] -= alam * a1;
         depls = fabs(alam) * sqrt(7. / 18);
     }
+    // (the reconstruction's products on the integer pipes, sf::mul)
+    using sf::mul;
     double ss00 = 0, ss11 = 0, ss22 = 0, ss01 = 0, ss02 = 0, ss12 = 0;
     for (int k = 0; k < 3; k++) {
-        ss00 += v[0][k] * v[0][k] * p[k];
-        ss01 += v[0][k] * v[1][k] * p[k];
-        ss02 += v[0][k] * v[2][k] * p[k];
-        ss11 += v[1][k] * v[1][k] * p[k];
-        ss12 += v[1][k] * v[2][k] * p[k];
-        ss22 += v[2][k] * v[2][k] * p[k];
+        ss00 += mul(mul(v[0][k], v[0][k]), p[k]);
+        ss01 += mul(mul(v[0][k], v[1][k]), p[k]);
+        ss02 += mul(mul(v[0][k], v[2][k]), p[k]);
+        ss11 += mul(mul(v[1][k], v[1][k]), p[k]);
+        ss12 += mul(mul(v[1][k], v[2][k]), p[k]);
+        ss22 += mul(mul(v[2][k], v[2][k]), p[k]);
     }
     s[0] = ss00;
     s[1] = ss11;
