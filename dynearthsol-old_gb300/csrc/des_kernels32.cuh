@@ -377,8 +377,8 @@ __device__ __forceinline__ void f_reference_force(const DevF &d, int e, const do
     const double s6 = sf::mul(d.s0[e], 1.0 / 6.0);
     const double buoy = d.F->gravity != 0.f ? sf::mul(d.F->mix[d.mix[e]].rho_g4, vol) : 0.0;
     for (int i = 0; i < 4; ++i) {
-        d.f0[(i)*E + e] = sf::mul(s6, cf[i][0]);
-        d.f0[(i + 4) * E + e] = sf::mul(s6, cf[i][1]);
+        d.f0[(i)*E + e] = s6 * cf[i][0];
+        d.f0[(i + 4) * E + e] = s6 * cf[i][1];
         d.f0[(i + 8) * E + e] = fma(s6, cf[i][2], buoy);
     }
 }
