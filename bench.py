@@ -476,7 +476,7 @@ def run_ours(args):
         dev32.step(nsteps)
         b = dev32.download(abi.State(mesh.nnode, mesh.nelem), abi.F_ALL)
         errs[f"after_{nsteps}_steps"] = compare(b, a)
-    e2e32, _, _ = e2e_rate(dev32, mesh, max(1, min(args.steps, 10)), barrier, world)
+    e2e32, _, _ = e2e_rate(dev32, mesh, max(1, min(args.steps, 20)), barrier, world)
     e2e32_ms = e2e_rate.last_ms
     dev32.close()
     dev.upload(S, abi.F_ALL)
@@ -576,7 +576,7 @@ def run_ours(args):
 
     # end to end through the drop-in entry point with page-locked host buffers:
     # every step uploads the loop's state from the host and downloads it back
-    e2e, h2d_bytes, d2h_bytes = e2e_rate(dev, mesh, max(1, min(args.steps, 10)), barrier, world)
+    e2e, h2d_bytes, d2h_bytes = e2e_rate(dev, mesh, max(1, min(args.steps, 20)), barrier, world)
     e2e_ms = e2e_rate.last_ms
 
     cb = None
