@@ -185,7 +185,7 @@ def e2e_rate(dev, mesh, steps, barrier, world):
     e2e_s = time.perf_counter() - t0
     D.unpin(host)
     e2e_rate.last_ms = {"min": 1e3 * min(per_step), "median": 1e3 * float(np.median(per_step)),
-                        "max": 1e3 * max(per_step)}
+                        "max": 1e3 * max(per_step), "slowest_step": int(np.argmax(per_step))}
     return world * mesh.nelem * steps / e2e_s, h2d, io_bytes
 
 
