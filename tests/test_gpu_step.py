@@ -132,7 +132,9 @@ def test_step_host_round_trip(gpu):
 def test_step_host_overlapped_downloads(gpu, precision, nsteps):
     """The fields finished before the last pass download on the second stream
     while that pass runs in element chunks, each chunk's rows downloading
-    while the next computes: every field and dt equal upload/step/download,
+    while the next computes; with one step, the stress pass's element inputs
+    also come up chunk by chunk on their own stream while it runs on the
+    chunks already landed.  Every field and dt equal upload/step/download,
     with the loop-state mask and page-locked host arrays, and with the output
     averaging switched on (it runs after the last pass)."""
     c = case("plastic")
