@@ -8,9 +8,13 @@ between timed steps.
 
   python bench.py [--gpus 1] [--steps K] [--warmup W] [--config 2] [--impl ours|reference]
 
---impl reference times the CPU implementation of the same loop (the oracle
-restatement, OpenMP on every host core; the reference's own objects are only
-available in the build container) on a bounded sample of the same workload.
+--impl reference times the CPU implementation of the same loop on the same
+workload, with the same --steps and --warmup (median of 3 timings of the
+steps): the oracle restatement with OpenMP on every host thread, its case
+built by the oracle alone (no product library is loaded).  The reference's own
+functions need its sources, which exist only where it is checked out; their
+speed against the restatement, measured there on the same threads
+(oracle/ref_speed.json), is reported beside the number.
 """
 import argparse
 import json
@@ -117,25 +121,48 @@ def build_case(cfg_key, box=None):
     return cfg, mesh, p, T, pls
 
 
-def cpu_baseline(cfg_key, steps=3, warmup=1):
-    """The CPU restatement (OpenMP, all host threads) on a bounded sample:
-    `steps` timed iterations of the full workload after `warmup`."""
+def cpu_baseline(cfg_key, steps=5, warmup=3, repeats=3):
+    """The CPU restatement of the loop (OpenMP, every host thread) on the same
+    workload, built by the oracle alone (oracle/workload_np.py: no product
+    library is loaded): `warmup` steps, then the median of `repeats` timings
+    of `steps` steps.  Beside it, the restatement's speed over the
+    reference's own functions measured on the same host, threads and case
+    where the reference's sources are (oracle/ref_speed.json)."""
+    import statistics
     from des_gb300 import workload as W
+    from oracle import workload_np as WN
     from oracle.oracle import PortOracle
-    cfg, mesh, p, T, pls = build_case(cfg_key)
-    o = PortOracle(mesh, p)
+    cfg = W.CONFIGS[cfg_key]
+    t0 = time.perf_counter()
+    mesh, p, T, pls, o = WN.setup_case(cfg)
     s = W.new_state(mesh, T, pls)
     o.init_fields(s)
+    setup_s = time.perf_counter() - t0
     if warmup:
         o.step(s, warmup)
-    t0 = time.perf_counter()
-    o.step(s, steps)
-    dt = time.perf_counter() - t0
-    from oracle.oracle import PortOracle as PO
-    threads = PO.lib().dso_num_threads()
-    return {"value": mesh.nelem * steps / dt, "unit": UNIT, "cores": int(threads), "kind": "port",
-            "sample": f"{steps} steps of {cfg.name} ({mesh.nelem} tets) after {warmup} warm-up, "
-                      f"{dt:.1f} s"}
+    times = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        o.step(s, steps)
+        times.append(time.perf_counter() - t0)
+    dt = statistics.median(times)
+    threads = int(PortOracle.lib().dso_num_threads())
+    out = {"value": mesh.nelem * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{cfg.name} ({mesh.nelem} tets): {warmup} warm-up steps, then the median of "
+                     f"{repeats} timings of {steps} steps ({', '.join(f'{x:.2f}' for x in times)} s); "
+                     f"case built in {setup_s:.1f} s by the oracle alone"}
+    f = ROOT / "oracle" / "ref_speed.json"
+    if f.exists():
+        r = json.loads(f.read_text())
+        out["reference_functions"] = {
+            "port_over_reference": r["port_over_reference"],
+            "estimate": out["value"] / r["port_over_reference"],
+            "measured": f"{r['case']}, {r['threads']} threads on {r['host']}: restatement "
+                        f"{r['port_elem_steps_per_s']:.3e}, reference's own functions "
+                        f"{r['reference_elem_steps_per_s']:.3e} element-steps/s",
+            "why": "the reference's sources are not on this host; the restatement is timed and "
+                   "the reference's own functions were timed against it where the sources are"}
+    return out
 
 
 def _fresh_form(cfg, precision, local, params=None):
@@ -346,33 +373,122 @@ def accuracy_2000(cfg_key, box, local, compare):
     return out
 
 
-def large_case_forms(args, local, world, reduce):
-    """Config 5 (400x400x80 hexes x 6 = 76.8M tets, three material layers,
-    elasto-visco-plastic): both forms, their device footprint and rate."""
+ACC_FIELDS = (("vel", "F_VEL"), ("stress", "F_STRESS"), ("temperature", "F_TEMPERATURE"),
+              ("strain", "F_STRAIN"), ("force", "F_FORCE"), ("coord", "F_COORD"),
+              ("plstrain", "F_PLSTRAIN"))
+
+
+def _field(dev, mesh, name, mask):
+    """One field of a device state (the other host arrays stay untouched)."""
+    from des_gb300 import abi
+    st = abi.State(mesh.nnode, mesh.nelem)
+    dev.download(st, mask)
+    return getattr(st, name)
+
+
+def long_run(cfg_key, checkpoints, local, world, reduce, rate_steps=10, sensitivity=True):
+    """Configs at their stated sizes over their stated step counts: the FP32
+    form and the FP64 form with its initial stress perturbed by 1e-12
+    (relative) -- the FP64 loop's own sensitivity, the yardstick for the
+    FP32 error -- against the FP64 form from the same initial state.  The
+    three run in lockstep on the device; at each checkpoint (steps from
+    init) the relative L2 of every compared field is formed field by field.
+    Each form's rate is timed with CUDA events over `rate_steps` steps after
+    3 warm-up steps (those steps count towards the checkpoints).  Without
+    `sensitivity` the perturbed FP64 form is left out."""
+    import numpy as np
     import des_gb300 as D
     from des_gb300 import abi, workload as W
-    cfg = W.CONFIGS["5"]
+    cfg = W.CONFIGS[cfg_key]
     t0 = time.perf_counter()
-    mesh, p, T, pls, topo = D.setup_case(cfg)
-    s0 = W.new_state(mesh, T, pls)
-    out = {"workload": f"{cfg.name}: {mesh.nelem} tets / {mesh.nnode} nodes, 3 layers, "
-                       "elasto-visco-plastic", "host_setup_s": time.perf_counter() - t0}
-    k = max(3, min(args.steps, 10))
-    for name, prec in (("fp64_plain", abi.PREC_FP64), ("fp32_mixed", abi.PREC_FP32)):
+    mesh, p, T, pls, _ = D.setup_case(cfg)
+    out = {"workload": f"{cfg.name}: {mesh.nelem} tets / {mesh.nnode} nodes, "
+                       f"{'elasto-visco-plastic' if cfg.rheology == 'evp' else 'elasto-plastic'}"
+                       f"{', %d material layers' % cfg.nlayers if cfg.nlayers > 1 else ''}"
+                       f"{', T noise sigma %g K' % cfg.t_sigma if cfg.t_sigma else ''}",
+           "host_setup_s": time.perf_counter() - t0}
+    devs = {}
+    names = [("fp64_plain", abi.PREC_FP64), ("fp32_mixed", abi.PREC_FP32)]
+    if sensitivity:
+        names.append(("fp64_perturbed", abi.PREC_FP64))
+    for name, prec in names:
         q = abi.Params.from_buffer_copy(p)
         q.precision = prec
         dv = D.Device(mesh, q, device=local)
-        dv.upload(s0, abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+        dv.upload(W.new_state(mesh, T, pls), abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
         dv.init_fields()
+        if name == "fp64_perturbed":
+            st = abi.State(mesh.nnode, mesh.nelem)
+            dv.download(st, abi.F_STRESS)
+            st.stress *= 1 + 1e-12
+            dv.upload(st, abi.F_STRESS)
+        devs[name] = dv
+    secs = {n: 0.0 for n in devs}
+    done = 0
+    for name, dv in devs.items():
+        if name == "fp64_perturbed":
+            dv.step(3 + rate_steps)
+            continue
         dv.step(3)
-        ms = dv.time_steps(k)
-        v, ms = replica_throughput(ms, mesh.nelem, k, world, reduce)
-        rep = dv.report()
-        out[name] = {"value": v, "ms_per_step": ms / k, "steps": k, "device_gb": dv.device_bytes / 1e9,
-                     "status": rep.status}
+        ms = dv.time_steps(rate_steps)
+        v, ms = replica_throughput(ms, mesh.nelem, rate_steps, world, reduce)
+        out[name] = {"value": v, "ms_per_step": ms / rate_steps, "device_gb": dv.device_bytes / 1e9}
+    done = 3 + rate_steps
+    reports = {}
+    for k in checkpoints:
+        for name, dv in devs.items():
+            t1 = time.perf_counter()
+            reports[name] = dv.step(k - done)
+            secs[name] += time.perf_counter() - t1
+        done = k
+        pairs = [("fp32_mixed", "fp32_vs_fp64")]
+        if sensitivity:
+            pairs.append(("fp64_perturbed", "fp64_perturbed_vs_fp64"))
+        errs = {key: {} for _, key in pairs}
+        for f, m in ACC_FIELDS:
+            ref = _field(devs["fp64_plain"], mesh, f, getattr(abi, m))
+            nb = float(np.linalg.norm(ref)) or 1.0
+            for name, key in pairs:
+                x = _field(devs[name], mesh, f, getattr(abi, m))
+                errs[key][f] = float(np.linalg.norm(x - ref)) / nb
+                del x
+            del ref
+        out[f"after_{k}_steps"] = errs
+    out["seconds_for_the_checkpointed_steps"] = secs
+    out["status"] = {n: r.status for n, r in reports.items()}
+    out["eigen_solves"] = {n: r.eigen_solves for n, r in reports.items()}
+    out["exact_returns_fp32"] = reports["fp32_mixed"].exact_returns
+    pls_end = _field(devs["fp64_plain"], mesh, "plstrain", abi.F_PLSTRAIN)
+    out["elements_whose_plastic_strain_grew_fp64"] = int(np.count_nonzero(pls_end > pls))
+    for dv in devs.values():
         dv.close()
     out["fp32_mixed"]["speedup_vs_fp64"] = out["fp32_mixed"]["value"] / out["fp64_plain"]["value"]
     return out
+
+
+def config4_returns(local, nsteps=2000):
+    """Config 4 as stated (the config-2 mesh, 9.6M tets, with config 3's
+    elasto-visco-plastic rheology): how many shear returns the FP64 form makes
+    over its 2,000 steps, i.e. how much work the learned closure would have."""
+    import numpy as np
+    import des_gb300 as D
+    from des_gb300 import abi, workload as W
+    cfg = W.CONFIGS["4"]
+    mesh, p, T, pls, _ = D.setup_case(cfg)
+    dv = D.Device(mesh, p, device=local)
+    dv.upload(W.new_state(mesh, T, pls), abi.F_COORD | abi.F_TEMPERATURE | abi.F_PLSTRAIN)
+    dv.init_fields()
+    t0 = time.perf_counter()
+    _, nret = dv.log_returns(nsteps, 1)
+    secs = time.perf_counter() - t0
+    r = dv.report()
+    grew = int(np.count_nonzero(_field(dv, mesh, "plstrain", abi.F_PLSTRAIN) > pls))
+    dv.close()
+    return {"workload": f"{cfg.name}: {mesh.nelem} tets / {mesh.nnode} nodes, config 3's "
+                        "elasto-visco-plastic rheology on the config-2 mesh with its weak-seed row",
+            "steps": nsteps, "shear_returns_fp64": int(nret), "eigen_solves_fp64": r.eigen_solves,
+            "elements_whose_plastic_strain_grew": grew, "status": r.status,
+            "seconds": secs}
 
 
 def workload_name(cfg):
@@ -382,21 +498,28 @@ def workload_name(cfg):
     return f"{cfg.name}: {nelem} tets / {nnode} nodes, elasto-plastic, FP64 plain form"
 
 
+def line_config(cfg, world):
+    """The line's config, identical in both arms."""
+    return {"workload": workload_name(cfg), "parallelism": f"replicas{world}",
+            "l2": "state 4.8 GB >> 129 MB L2, no flush"}
+
+
 def run_reference(args):
+    """The CPU implementation of the loop on the same workload, steps and
+    warm-up as the GPU arm (rank 0 only under torchrun)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    # bounded sample: at most 5 timed steps of the full mesh after 1 warm-up step
     from des_gb300 import workload as W
-    steps = min(args.steps, 5)
     cfg = W.CONFIGS[args.config]
-    cb = cpu_baseline(args.config, steps=steps, warmup=1)
+    cb = cpu_baseline(args.config, steps=args.steps, warmup=args.warmup, repeats=3)
+    nelem = 6 * cfg.nx * cfg.ny * cfg.nz
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
-            "n_gpus": args.gpus, "steps": steps, "warmup": 1,
-            "ms_per_step": 6 * cfg.nx * cfg.ny * cfg.nz / cb["value"] * 1e3,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": nelem / cb["value"] * 1e3,
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": workload_name(cfg), "parallelism": f"host threads {cb['cores']}"},
+            "config": line_config(cfg, args.gpus),
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -494,9 +617,11 @@ def run_ours(args):
                                            torch_reduce_max(f"cuda:{local}") if dist else None, compare)
     if not args.no_accuracy and world == 1:
         forms["fp32_accuracy_2000_steps"] = accuracy_2000(args.config, args.box, local, compare)
+    red = torch_reduce_max(f"cuda:{local}") if dist else None
     if not args.no_large:
-        forms["config5"] = large_case_forms(args, local, world,
-                                            torch_reduce_max(f"cuda:{local}") if dist else None)
+        forms["config3"] = long_run("3", (100, 1000, 5000), local, world, red)
+        forms["config4"] = config4_returns(local)
+        forms["config5"] = long_run("5", (100, 1000), local, world, red, sensitivity=False)
 
     # per-pass device times over extra steps (same arithmetic, launched one by one)
     prof_steps = max(2, min(args.steps, 5))
@@ -581,14 +706,13 @@ def run_ours(args):
 
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(args.config, steps=2, warmup=1)
+        cb = cpu_baseline(args.config, steps=5, warmup=3, repeats=3)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": workload_name(cfg),
-                   "parallelism": f"replicas{world}", "l2": "state 4.8 GB >> 129 MB L2, no flush"},
+        "config": line_config(cfg, world),
         "gpu_launches": dev.kernels_per_step * args.steps,
         "roofline": {"bound": "hbm", "kernel": names[top], "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm,
@@ -639,7 +763,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-yielding", action="store_true",
                     help="skip the forms on the yielding workload")
-    ap.add_argument("--no-large", action="store_true", help="skip config 5 (76.8M tets)")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip configs 3, 4 and 5 at their stated sizes and step counts")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the 2,000-step FP32-against-FP64 accuracy run")
     ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure"], default=None,

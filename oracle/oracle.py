@@ -24,6 +24,8 @@ from des_gb300 import abi  # noqa: E402
 
 PORT_LIB = ORACLE / "_build" / "libdes_oracle.so"
 REF_LIB = ORACLE / "_ref" / "libdesref.so"
+# the reference checkout the CPU checkers read (DES_REFERENCE overrides the
+# build container's location; where neither exists the checks that need it skip)
 REF_SRC = Path(os.environ.get("DES_REFERENCE", "/root/reference"))
 
 FUNCTIONS = ["update_temperature", "update_strain_rate", "compute_dvoldt", "compute_edvoldt",

@@ -5,8 +5,11 @@
 # -O3 -ffast-math as 3x3-C/Makefile sets; TetGen predicates at -O0; Triangle at
 # -O1).  input.cxx (boost) and dynearthsol.cxx (main) are not built.
 #
-#   make -f oracle/ref.mk REF=/root/reference -j8
-REF    ?= /root/reference
+#   make -f oracle/ref.mk REF=<reference tree> -j8     (oracle.build_ref() passes it)
+REF    ?=
+ifeq ($(REF),)
+$(error REF=<reference tree> is required)
+endif
 OUT    := oracle/_ref
 OBJ    := $(OUT)/obj
 CXX    ?= g++
