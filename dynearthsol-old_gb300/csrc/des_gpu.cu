@@ -2209,6 +2209,51 @@ int des_gpu_compute_dt(des_gpu *g, double *dt_out)
     return (c.dt > 0) ? DES_OK : DES_ERR_DT;
 }
 
+// compute_volume on caller arrays in the reference layout (AoS coordinates)
+__global__ void k_volume_rows(int nelem, const double *__restrict__ coord,
+                              const int4 *__restrict__ conn, double *__restrict__ vol)
+{
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nelem) return;
+    int4 q = conn[e];
+    const int n[4] = {q.x, q.y, q.z, q.w};
+    double X[4][3];
+    for (int i = 0; i < 4; ++i)
+        for (int k = 0; k < 3; ++k) X[i][k] = coord[3LL * n[i] + k];
+    vol[e] = tet_volume(X[0], X[1], X[2], X[3]);
+}
+
+int des_compute_volume(int nnode, int nelem, const double *coord, const int *connectivity,
+                       double *volume)
+{
+    if (nnode < 1 || nelem < 1 || !coord || !connectivity || !volume) return DES_ERR_ARG;
+    double *dx = nullptr, *dv = nullptr;
+    int *dc = nullptr;
+    cudaStream_t s = nullptr;
+    int rc = cuda_rc(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    if (!rc && (cudaMalloc(&dx, sizeof(double) * 3 * (size_t)nnode) != cudaSuccess ||
+                cudaMalloc(&dc, sizeof(int) * 4 * (size_t)nelem) != cudaSuccess ||
+                cudaMalloc(&dv, sizeof(double) * (size_t)nelem) != cudaSuccess))
+        rc = DES_ERR_NOMEM;
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(dx, coord, sizeof(double) * 3 * (size_t)nnode,
+                                          cudaMemcpyHostToDevice, s));
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(dc, connectivity, sizeof(int) * 4 * (size_t)nelem,
+                                          cudaMemcpyHostToDevice, s));
+    if (!rc) {
+        k_volume_rows<<<blocks(nelem, kElemBlock), kElemBlock, 0, s>>>(
+            nelem, dx, reinterpret_cast<const int4 *>(dc), dv);
+        rc = cuda_rc(cudaGetLastError());
+    }
+    if (!rc) rc = cuda_rc(cudaMemcpyAsync(volume, dv, sizeof(double) * (size_t)nelem,
+                                          cudaMemcpyDeviceToHost, s));
+    if (!rc) rc = cuda_rc(cudaStreamSynchronize(s));
+    cudaFree(dx);
+    cudaFree(dc);
+    cudaFree(dv);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+}
+
 static int init_fields_fp32(des_gpu *g)
 {
     const size_t N = g->nnode, E = g->nelem;

@@ -18,8 +18,15 @@
 //    host threads without ordering) race and give wrong results; the counter
 //    is cleared at the start of every call, the partials are rewritten by it.
 //  * the first call on a device looks up the array's device address (a
-//    one-time set-up per device, done with that device current); make that
-//    first call before any stream capture.
+//    set-up per device, done with that device current); make that first
+//    call before any stream capture.  Every later call made while its stream
+//    is not capturing looks the address up again, so a device reset (which
+//    unloads the library's module and may place the array elsewhere when it
+//    is loaded again) is followed by a fresh look-up; a call made during a
+//    capture uses the address of the last call made outside one.
+//  * dt <= 0, where compute_dt exits with code 11 (geometry.cxx:321-325),
+//    is reported through the optional device status word, which every call
+//    sets to DES_OK or DES_ERR_DT.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -90,7 +97,7 @@ __global__ void __launch_bounds__(kBlock) k_dt_noalloc(unsigned long long *scrat
                                                        const int4 *__restrict__ conn,
                                                        const double *__restrict__ vol,
                                                        const double *__restrict__ shearm, DtIn c,
-                                                       double *dt_out)
+                                                       double *dt_out, int *status)
 {
     __shared__ bool last;
     int e = blockIdx.x * kBlock + threadIdx.x;
@@ -133,27 +140,41 @@ __global__ void __launch_bounds__(kBlock) k_dt_noalloc(unsigned long long *scrat
         double dt_advection = 0.5 * minl / c.max_vbc_val;
         double dt_elastic = c.is_qs ? 0.5 * minl / (c.max_vbc_val * c.inertial_scaling)
                                     : 0.5 * minl / sqrt(c.bulkm0 / c.rho0);
-        *dt_out = smin(smin(dt_elastic, dt_maxwell), smin(dt_advection, dt_diffusion)) * c.dt_fraction;
+        double dt = smin(smin(dt_elastic, dt_maxwell), smin(dt_advection, dt_diffusion)) * c.dt_fraction;
+        *dt_out = dt;
+        if (status) *status = (dt <= 0) ? DES_ERR_DT : DES_OK;
         scratch[kCounter] = 0;
     }
 }
 
-__global__ void k_dt_fixed(double *dt_out, double v)
+__global__ void k_dt_fixed(double *dt_out, double v, int *status)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) *dt_out = v;
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        *dt_out = v;
+        if (status) *status = DES_OK;     // compute_dt returns a fixed dt unchecked
+    }
 }
 
 std::mutex g_setup_mutex;
 unsigned long long *g_scratch_ptr[kMaxDevices] = {nullptr};
 
-// device address of g_dt_scratch on the current device (set-up once per device)
-int scratch_address(unsigned long long **out)
+// Device address of g_dt_scratch on the current device.  Looked up (with the
+// device current) on the first call and on every call whose stream is not
+// capturing; a capturing call uses the address its device had last.
+int scratch_address(cudaStream_t s, unsigned long long **out)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return DES_ERR_CUDA;
     if (dev < 0 || dev >= kMaxDevices) return DES_ERR_UNSUPPORTED;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusActive;
+    bool capturing = true;
+    if (cudaStreamIsCapturing(s, &cap) == cudaSuccess)
+        capturing = cap != cudaStreamCaptureStatusNone;
+    else
+        (void)cudaGetLastError();   // the legacy stream while another captures: not sticky
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    if (!capturing || !g_scratch_ptr[dev]) {
+        if (capturing) return DES_ERR_UNSUPPORTED;   // no set-up outside a capture yet
         void *p = nullptr;
         if (cudaGetSymbolAddress(&p, g_dt_scratch) != cudaSuccess || !p) return DES_ERR_CUDA;
         g_scratch_ptr[dev] = static_cast<unsigned long long *>(p);
@@ -166,19 +187,20 @@ int scratch_address(unsigned long long **out)
 
 extern "C" int des_compute_dt_noalloc(int nelem, const double *coord, const int *connectivity,
                                       const double *volume, const double *shearm,
-                                      const des_dt_inputs *in, double *dt, void *stream)
+                                      const des_dt_inputs *in, double *dt, int *status,
+                                      void *stream)
 {
     if (!in || !dt) return DES_ERR_ARG;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (in->fixed_dt != 0) {
-        k_dt_fixed<<<1, 32, 0, s>>>(dt, in->fixed_dt);
+        k_dt_fixed<<<1, 32, 0, s>>>(dt, in->fixed_dt, status);
         return cudaGetLastError() == cudaSuccess ? DES_OK : DES_ERR_CUDA;
     }
     if (nelem < 1 || !coord || !connectivity || !volume) return DES_ERR_ARG;
     if (reinterpret_cast<uintptr_t>(connectivity) % 16 != 0) return DES_ERR_ARG;
     if (nelem > kMaxElems) return DES_ERR_SIZE;
     unsigned long long *scratch = nullptr;
-    int rc = scratch_address(&scratch);
+    int rc = scratch_address(s, &scratch);
     if (rc) return rc;
     if (cudaMemsetAsync(scratch + kCounter, 0, sizeof(unsigned long long), s) != cudaSuccess)
         return DES_ERR_CUDA;
@@ -196,6 +218,6 @@ extern "C" int des_compute_dt_noalloc(int nelem, const double *coord, const int 
     int grid = (int)((nelem + kBlock - 1) / kBlock);
     k_dt_noalloc<<<grid, kBlock, 0, s>>>(scratch, nelem, coord,
                                           reinterpret_cast<const int4 *>(connectivity), volume,
-                                          shearm, c, dt);
+                                          shearm, c, dt, status);
     return cudaGetLastError() == cudaSuccess ? DES_OK : DES_ERR_CUDA;
 }

@@ -72,7 +72,7 @@ def lib():
     L.des_abi_sizes.argtypes = [P(C.c_longlong)]
     L.des_abi_sizes.restype = None
     L.des_compute_dt_noalloc.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                         P(abi.DtInputs), C.c_void_p, C.c_void_p]
+                                         P(abi.DtInputs), C.c_void_p, C.c_void_p, C.c_void_p]
     fp = P(C.c_float)
     L.des_mlp_forward.argtypes = [P(abi.Mlp), fp, C.c_longlong, fp]
     L.des_mlp_loss_grad.argtypes = [P(abi.Mlp), fp, fp, C.c_longlong, P(C.c_double), P(abi.Mlp)]

@@ -305,6 +305,15 @@ int  des_gpu_update_mesh(des_gpu *g);          /* dynearthsol.cxx:237-261 */
 int  des_gpu_rotate_stress(des_gpu *g);        /* fields.cxx:455-533 */
 int  des_gpu_compute_dt(des_gpu *g, double *dt_out);   /* geometry.cxx:257-330; also stores dt */
 
+/* compute_volume (geometry.cxx:86-114) of any mesh given as host arrays in the
+ * reference layout (coord [nnode][3], connectivity [nelem][4]) into host
+ * volume[nelem], without a handle: the reference also calls it on meshes and
+ * volume arrays that are not the loop's (markerset.cxx:238, remeshing.cxx:1069).
+ * Copies the arrays to temporary device buffers, computes, copies back
+ * (synchronous). */
+int  des_compute_volume(int nnode, int nelem, const double *coord, const int *connectivity,
+                        double *volume);
+
 /* ---- learned return-map closure (no reference counterpart) -------------- */
 /* A 14 -> 64 -> 64 -> 7 MLP with ReLU (inputs padded to 16, outputs to 8),
  * BF16 weights and activations with FP32 accumulation on the tensor cores.
@@ -449,13 +458,17 @@ typedef struct des_dt_inputs {
  * the reference layout -- coord [nnode][3], connectivity [nelem][4] (16-byte
  * aligned), volume [nelem], optional per-element shear modulus -- and writes
  * it to the device double *dt, on `stream` (NULL: default stream), without
- * allocating anything.  Its scratch is a fixed array inside the library:
- * nelem is limited to 16,777,216 (DES_ERR_SIZE above), calls that overlap on
- * the GPU race, and the first call on a device does a one-time set-up of the
- * array's address (make it before any stream capture). */
+ * allocating anything.  `status` (a device int, may be NULL) receives DES_OK,
+ * or DES_ERR_DT where compute_dt would exit with code 11 (dt <= 0,
+ * geometry.cxx:321-325); read it after the stream has run the call.  Its
+ * scratch is a fixed array inside the library: nelem is limited to
+ * 16,777,216 (DES_ERR_SIZE above), calls that overlap on the GPU race, and
+ * the first call on a device sets up the array's address (make it before any
+ * stream capture; calls made outside a capture look the address up again, so
+ * a device reset needs nothing more than one such call). */
 int  des_compute_dt_noalloc(int nelem, const double *coord, const int *connectivity,
                             const double *volume, const double *shearm,
-                            const des_dt_inputs *in, double *dt, void *stream);
+                            const des_dt_inputs *in, double *dt, int *status, void *stream);
 
 /* ---- measurement (no reference counterpart) ----------------------------- */
 /* Runs nsteps graph launches between two CUDA events on the handle's stream
