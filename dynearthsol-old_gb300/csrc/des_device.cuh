@@ -77,17 +77,27 @@ __device__ __forceinline__ R second_invariant2(const R *t)
 
 // ---- MatProps -------------------------------------------------------------
 
-// element mean temperature (matprops.cxx:613-618)
+// Exact steps in the element's arithmetic type: for FP64 on the integer
+// pipes (0 + x, 2 x, x / 4, x / 3 as the FP64 unit rounds them, sf::*), for
+// FP32 the FP32 instructions themselves
+__device__ __forceinline__ double padd0(double x) { return sf::add0(x); }
+__device__ __forceinline__ float padd0(float x) { return 0.f + x; }
+__device__ __forceinline__ double ptwice(double x) { return sf::twice(x); }
+__device__ __forceinline__ float ptwice(float x) { return 2 * x; }
+__device__ __forceinline__ double pquarter(double x) { return sf::quarter(x); }
+__device__ __forceinline__ float pquarter(float x) { return x / 4; }
+__device__ __forceinline__ double pdiv3(double x) { return sf::div3(x); }
+__device__ __forceinline__ float pdiv3(float x) { return x / 3; }
+
+// element mean temperature (matprops.cxx:613-618): ((((0 + a) + b) + c) + d) / 4
 template <class R>
 __device__ __forceinline__ R elem_mean4(R a, R b, R c, R d)
 {
-    R t = 0;
-    t += a;
+    R t = padd0(a);
     t += b;
     t += c;
     t += d;
-    t /= 4;
-    return t;
+    return pquarter(t);
 }
 
 // matprops.cxx:707-728
@@ -418,7 +428,7 @@ __device__ __forceinline__ void elastic(R bulkm, R shearm, const R *de, R *s)
 {
     R lambda = bulkm - R(2.) / R(3) * shearm;
     R dev = tr3(de);
-    const R g2 = 2 * shearm;
+    const R g2 = ptwice(shearm);
     for (int i = 0; i < 3; ++i) s[i] += pmul(g2, de[i]) + pmul(lambda, dev);
     for (int i = 3; i < 6; ++i) s[i] += pmul(g2, de[i]);
 }
@@ -429,19 +439,21 @@ __device__ __forceinline__ void maxwell(R bulkm, R shearm, R viscosity, R dt, R 
     R tmp = R(0.5) * dt * shearm / viscosity;
     R f1 = 1 - tmp;
     R f2 = 1 / (1 + tmp);
-    R dev = tr3(de) / 3;
-    R s0 = tr3(s) / 3;
+    R dev = pdiv3(tr3(de));
+    R s0 = pdiv3(tr3(s));
+    const R g2 = ptwice(shearm);
     for (int i = 0; i < 3; ++i)
-        s[i] = ((s[i] - s0) * f1 + 2 * shearm * (de[i] - dev)) * f2 + s0 + bulkm * dv;
-    for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + 2 * shearm * de[i]) * f2;
+        s[i] = ((s[i] - s0) * f1 + g2 * (de[i] - dev)) * f2 + s0 + bulkm * dv;
+    for (int i = 3; i < 6; ++i) s[i] = (s[i] * f1 + g2 * de[i]) * f2;
 }
 
 template <class R>
 __device__ __forceinline__ void viscous(R bulkm, R viscosity, R total_dv, const R *edot, R *s)
 {
-    R dev = tr3(edot) / 3;
-    for (int i = 0; i < 3; ++i) s[i] = 2 * viscosity * (edot[i] - dev) + bulkm * total_dv;
-    for (int i = 3; i < 6; ++i) s[i] = 2 * viscosity * edot[i];
+    R dev = pdiv3(tr3(edot));
+    const R v2 = ptwice(viscosity);
+    for (int i = 0; i < 3; ++i) s[i] = v2 * (edot[i] - dev) + bulkm * total_dv;
+    for (int i = 3; i < 6; ++i) s[i] = v2 * edot[i];
 }
 
 // Conservative test that the reference's composite yield check
@@ -605,8 +617,9 @@ __device__ __forceinline__ double tet_volume(const double *d0, const double *d1,
     double z01 = d0[2] - d1[2];
     double z12 = d1[2] - d2[2];
     double z23 = d2[2] - d3[2];
-    return (x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) +
-            x23 * (y12 * z01 - y01 * z12)) / 6;
+    // (the division by 6 on the integer pipes, sf::div6)
+    return sf::div6(x01 * (y23 * z12 - y12 * z23) + x12 * (y01 * z23 - y23 * z01) +
+                    x23 * (y12 * z01 - y01 * z12));
 }
 
 // geometry.cxx:53-83 (3D)
@@ -693,47 +706,61 @@ __device__ __forceinline__ void spin(const R V[4][3], const R *dx, const R *dy, 
 // 0.5 is exact and commutes with rounding, so 0.5 times the sum of the
 // brackets equals the reference's sum bit for bit (for terms above the
 // subnormal range).
+//
+// Each sum starts from zero in the reference; its first addition, 0 + x, is
+// x except for -0 and is formed on the integer pipes (sf::add0), as are the
+// exact scalings by 0.5 (sf::half).
 __device__ __forceinline__ void spin_and_rate(const double V[4][3], const double *dx, const double *dy,
                                               const double *dz, double &w3, double &w4, double &w5,
                                               double D[6])
 {
-    D[0] = 0;
-    for (int i = 0; i < 4; ++i) D[0] += V[i][0] * dx[i];
-    D[1] = 0;
-    for (int i = 0; i < 4; ++i) D[1] += V[i][1] * dy[i];
-    D[2] = 0;
-    for (int i = 0; i < 4; ++i) D[2] += V[i][2] * dz[i];
-    double t3 = 0, t4 = 0, t5 = 0, u3 = 0, u4 = 0, u5 = 0;
+    D[0] = sf::add0(V[0][0] * dx[0]);
+    for (int i = 1; i < 4; ++i) D[0] += V[i][0] * dx[i];
+    D[1] = sf::add0(V[0][1] * dy[0]);
+    for (int i = 1; i < 4; ++i) D[1] += V[i][1] * dy[i];
+    D[2] = sf::add0(V[0][2] * dz[0]);
+    for (int i = 1; i < 4; ++i) D[2] += V[i][2] * dz[i];
+    double t3, t4, t5, u3, u4, u5;
+#pragma unroll
     for (int i = 0; i < 4; ++i) {
         const double xy = V[i][0] * dy[i], yx = V[i][1] * dx[i];
         const double xz = V[i][0] * dz[i], zx = V[i][2] * dx[i];
         const double yz = V[i][1] * dz[i], zy = V[i][2] * dy[i];
-        t3 += xy + yx;
-        u3 += xy - yx;
-        t4 += xz + zx;
-        u4 += xz - zx;
-        t5 += yz + zy;
-        u5 += yz - zy;
+        if (i == 0) {
+            t3 = sf::add0(xy + yx);
+            u3 = sf::add0(xy - yx);
+            t4 = sf::add0(xz + zx);
+            u4 = sf::add0(xz - zx);
+            t5 = sf::add0(yz + zy);
+            u5 = sf::add0(yz - zy);
+        } else {
+            t3 += xy + yx;
+            u3 += xy - yx;
+            t4 += xz + zx;
+            u4 += xz - zx;
+            t5 += yz + zy;
+            u5 += yz - zy;
+        }
     }
-    D[3] = 0.5 * t3;
-    D[4] = 0.5 * t4;
-    D[5] = 0.5 * t5;
-    w3 = 0.5 * u3;
-    w4 = 0.5 * u4;
-    w5 = 0.5 * u5;
+    D[3] = sf::half(t3);
+    D[4] = sf::half(t4);
+    D[5] = sf::half(t5);
+    w3 = sf::half(u3);
+    w4 = sf::half(u4);
+    w5 = sf::half(u5);
 }
 
 // fields.cxx:419-433 in FP64: the reference's 2 s_ab w products appear twice
 // each; 2 (s_ab w) is formed once per pair and the factor 2 applied to the
-// sum (exact, as above)
+// sum (exact, as above; an exponent step on the integer pipes, sf::twice)
 __device__ __forceinline__ void jaumann64(double *s, double dt, double w3, double w4, double w5)
 {
     // (products on the integer pipes, sf::mul)
     const double p3 = sf::mul(s[3], w3), p4 = sf::mul(s[4], w4), p5 = sf::mul(s[5], w5);
     double inc[6];
-    inc[0] = 2.0 * (-p3 - p4);
-    inc[1] = 2.0 * (p3 - p5);
-    inc[2] = 2.0 * (p4 + p5);
+    inc[0] = sf::twice(-p3 - p4);
+    inc[1] = sf::twice(p3 - p5);
+    inc[2] = sf::twice(p4 + p5);
     inc[3] = sf::mul(s[0], w3) - sf::mul(s[1], w3) - sf::mul(s[4], w5) - sf::mul(s[5], w4);
     inc[4] = sf::mul(s[0], w4) - sf::mul(s[2], w4) + sf::mul(s[3], w5) - sf::mul(s[5], w3);
     inc[5] = sf::mul(s[1], w5) - sf::mul(s[2], w5) + sf::mul(s[3], w4) + sf::mul(s[4], w3);
@@ -767,9 +794,11 @@ __device__ __forceinline__ void conduction(const double *dx, const double *dy, c
             D[i][j] = sf::mul(dx[i], dx[j]) + sf::mul(dy[i], dy[j]) + sf::mul(dz[i], dz[j]);
             D[j][i] = D[i][j];
         }
+    // (the loops stay rolled: in E-A the shorter code runs faster than the
+    // matrix held in registers, which unrolling them would give)
     for (int i = 0; i < 4; ++i) {
-        double diffusion = 0.;
-        for (int j = 0; j < 4; ++j) diffusion += sf::mul(D[i][j], Tn[j]);
+        double diffusion = sf::add0(sf::mul(D[i][0], Tn[0]));    // 0 + x (sf::add0)
+        for (int j = 1; j < 4; ++j) diffusion += sf::mul(D[i][j], Tn[j]);
         tr[i] = sf::mul(diffusion, kv);
     }
 }

@@ -12,6 +12,8 @@
 
 #include "des_gpu.h"
 #include "des_closure.cuh"
+#include "des_support.cuh"
+#include "des_topology.h"
 
 using namespace des;
 
@@ -717,10 +719,12 @@ __device__ __forceinline__ unsigned long long check_mix(unsigned long long z)
     return z ^ (z >> 31);
 }
 
-// sf::mul and sf::to_float against the FP64 unit's multiply and conversion
+// sf::mul, sf::to_float, sf::add0, sf::twice, sf::half, sf::div6, sf::div3
+// and sf::quarter against the FP64 unit's multiply, conversion, addition and
+// division
 __global__ void k_softf64_check(unsigned long long *bad, long long n, unsigned long long seed)
 {
-    unsigned long long nb[4] = {0, 0, 0, 0};
+    unsigned long long nb[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
         const unsigned long long r1 = check_mix(seed + 2 * i + 1), r2 = check_mix(seed + 2 * i + 2);
@@ -729,6 +733,8 @@ __global__ void k_softf64_check(unsigned long long *bad, long long n, unsigned l
         const double x1 = sf::from_bits((r1 & keep) | ((963ull + r2 % 121) << 52));
         const double y1 = sf::from_bits((r2 & keep) | ((963ull + (r1 >> 7) % 121) << 52));
         const double xf = sf::from_bits((r1 & keep) | ((870ull + (r2 >> 11) % 310) << 52));
+        // every other operand with an exponent field of 0-8 (subnormals, results near them)
+        const double xs = (i & 1) ? x : sf::from_bits((r1 & keep) | ((r2 % 9) << 52));
         double h = __dmul_rn(x, y), g = sf::mul(x, y);
         nb[0] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
         h = __dmul_rn(x1, y1);
@@ -739,8 +745,26 @@ __global__ void k_softf64_check(unsigned long long *bad, long long n, unsigned l
         hf = __double2float_rn(xf);
         gf = sf::to_float(xf);
         nb[3] += __float_as_uint(hf) != __float_as_uint(gf);
+        h = __dadd_rn(0.0, xs);
+        g = sf::add0(xs);
+        nb[4] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __dmul_rn(xs, 2.0);
+        g = sf::twice(xs);
+        nb[5] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __dmul_rn(xs, 0.5);
+        g = sf::half(xs);
+        nb[6] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __ddiv_rn(xs, 6.0);
+        g = sf::div6(xs);
+        nb[7] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __ddiv_rn(xs, 3.0);
+        g = sf::div3(xs);
+        nb[8] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
+        h = __dmul_rn(xs, 0.25);
+        g = sf::quarter(xs);
+        nb[9] += sf::bits(h) != sf::bits(g) && !(h != h && g != g);
     }
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < 10; ++k)
         if (nb[k]) atomicAdd(bad + k, nb[k]);
 }
 
@@ -748,20 +772,20 @@ __global__ void k_softf64_check(unsigned long long *bad, long long n, unsigned l
 
 extern "C" {
 
-int des_gpu_softf64_check(int device, long long n, unsigned long long seed, unsigned long long mismatches[4])
+int des_gpu_softf64_check(int device, long long n, unsigned long long seed, unsigned long long mismatches[10])
 {
     if (n < 0 || !mismatches) return DES_ERR_ARG;
     DES_CUDA(cudaSetDevice(device));
     unsigned long long *bad = nullptr;
-    DES_CUDA(cudaMalloc(&bad, 4 * sizeof(unsigned long long)));
-    cudaError_t e = cudaMemset(bad, 0, 4 * sizeof(unsigned long long));
+    DES_CUDA(cudaMalloc(&bad, 10 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemset(bad, 0, 10 * sizeof(unsigned long long));
     int sms = 0;
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) {
         k_softf64_check<<<sms * 8, 256>>>(bad, n, seed);
         e = cudaGetLastError();
     }
-    if (e == cudaSuccess) e = cudaMemcpy(mismatches, bad, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(mismatches, bad, 10 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
     cudaFree(bad);
     return cuda_rc(e);
 }
@@ -782,13 +806,43 @@ const char *des_gpu_error_string(int code)
     }
 }
 
+// create_support (mesh.cxx:1703-1717) from the device connectivity into the
+// CSR the node passes gather over (des_support.cuh)
+static int build_support(des_gpu *g, const int *conn, int *sup_off, unsigned *sup_ent)
+{
+    const int N = g->nnode;
+    const long long nent = 4LL * g->nelem, n1 = (long long)N + 1;
+    const int nb = (int)((n1 + kScanBlock - 1) / kScanBlock);
+    cudaStream_t s = g->stream;
+    int *sums = nullptr, *cursor = nullptr;
+    int rc = DES_OK;
+    if (cudaMalloc(&sums, sizeof(int) * (size_t)nb) != cudaSuccess ||
+        cudaMalloc(&cursor, sizeof(int) * (size_t)N) != cudaSuccess)
+        rc = DES_ERR_NOMEM;
+    if (!rc) rc = cuda_rc(cudaMemsetAsync(sup_off, 0, sizeof(int) * (size_t)n1, s));
+    if (!rc) rc = cuda_rc(cudaMemsetAsync(cursor, 0, sizeof(int) * (size_t)N, s));
+    if (!rc) {
+        k_sup_count<<<blocks(nent, 256), 256, 0, s>>>(nent, conn, sup_off);
+        k_scan_blocks<<<nb, kScanBlock, 0, s>>>(sup_off, n1, sums);
+        k_scan_sums<<<1, kScanBlock, 0, s>>>(sums, nb);
+        k_scan_add<<<nb, kScanBlock, 0, s>>>(sup_off, n1, sums);
+        k_sup_fill<<<blocks(nent, 256), 256, 0, s>>>(nent, conn, sup_off, cursor, sup_ent);
+        k_sup_sort<<<blocks(N, kNodeBlock), kNodeBlock, 0, s>>>(N, sup_off, sup_ent);
+        rc = cuda_rc(cudaGetLastError());
+    }
+    if (!rc) rc = cuda_rc(cudaStreamSynchronize(s));
+    cudaFree(sums);
+    cudaFree(cursor);
+    return rc;
+}
+
 int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_gpu **out)
 {
     if (!m || !p || !out || !m->elemmarkers) return DES_ERR_ARG;
     int rc = check_params(*p, m->nmat);
     if (rc) return rc;
     des_topology *topo = nullptr;
-    rc = des_topology_build(m, &topo);
+    rc = topology_build(m, &topo, false);   // support lists: built on the device below
     if (rc) return rc;
     des_gpu *g = new (std::nothrow) des_gpu();   // value-initialised: every device pointer starts null
     if (!g) {
@@ -954,15 +1008,11 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
         g->f.bf = sb;
     }
 
-    std::vector<unsigned> ent(4 * E);
-    for (size_t q = 0; q < 4 * E; ++q)
-        ent[q] = ((unsigned)topo->support_elems[q] << 2) | (unsigned)topo->support_slots[q];
     if (cudaMemcpy(conn, m->connectivity, sizeof(int) * 4 * E, cudaMemcpyHostToDevice) ||
-        cudaMemcpy(sup_off, topo->support_offsets, sizeof(int) * (N + 1), cudaMemcpyHostToDevice) ||
-        cudaMemcpy(sup_ent, ent.data(), sizeof(unsigned) * 4 * E, cudaMemcpyHostToDevice) ||
         cudaMemcpy(bcflag, topo->bcflag, sizeof(unsigned) * N, cudaMemcpyHostToDevice) ||
         cudaMemcpy(dmix, mix.data(), E, cudaMemcpyHostToDevice))
         return fail(DES_ERR_CUDA);
+    if ((rc = build_support(g, reinterpret_cast<const int *>(conn), sup_off, sup_ent))) return fail(rc);
     des_topology_free(topo);
     topo = nullptr;
     Clock c0;
@@ -973,6 +1023,21 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
         return fail(DES_ERR_CUDA);
     if ((rc = build_consts(g))) return fail(rc);
     *out = g;
+    return DES_OK;
+}
+
+int des_gpu_download_support(des_gpu *g, int *offsets, int *elems, int *slots)
+{
+    if (!g || !offsets || !elems || !slots) return DES_ERR_ARG;
+    const size_t N = g->nnode, E = g->nelem;
+    std::vector<unsigned> ent(4 * E);
+    DES_CUDA(cudaStreamSynchronize(g->stream));
+    DES_CUDA(cudaMemcpy(offsets, g->d.sup_off, sizeof(int) * (N + 1), cudaMemcpyDeviceToHost));
+    DES_CUDA(cudaMemcpy(ent.data(), g->d.sup_ent, sizeof(unsigned) * 4 * E, cudaMemcpyDeviceToHost));
+    for (size_t q = 0; q < 4 * E; ++q) {
+        elems[q] = (int)(ent[q] >> 2);
+        slots[q] = (int)(ent[q] & 3u);
+    }
     return DES_OK;
 }
 

@@ -191,7 +191,8 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
     double old_s = tr3(s);
     {
         double div = tr3(edot);
-        for (int i = 0; i < 3; ++i) edot[i] += (edv - div) / 3;
+        const double corr = sf::div3(edv - div);
+        for (int i = 0; i < 3; ++i) edot[i] += corr;
     }
     // (products on the integer pipes, sf::mul)
     double de[6];
@@ -576,9 +577,9 @@ __global__ void k_edvoldt(Dev d)
     if (e >= d.nelem) return;
     double a[4];
     load_nodal4(d.ntmp, d.conn[e], a);
-    double dj = 0;
-    for (int i = 0; i < 4; ++i) dj += a[i];
-    d.edvoldt[e] = dj / 4;
+    double dj = sf::add0(a[0]);
+    for (int i = 1; i < 4; ++i) dj += a[i];
+    d.edvoldt[e] = sf::quarter(dj);
 }
 
 // rheology.cxx:525-650
@@ -613,10 +614,10 @@ __global__ void k_nmd_apply(Dev d)
     const size_t E = d.nelem;
     double a[4];
     load_nodal4(d.ntmp, d.conn[e], a);
-    double dpe = 0;
-    for (int i = 0; i < 4; ++i) dpe += a[i];
-    double dp_el = dpe / 4;
-    double ddp = (-d.dp[e] + dp_el) / 3;
+    double dpe = sf::add0(a[0]);
+    for (int i = 1; i < 4; ++i) dpe += a[i];
+    double dp_el = sf::quarter(dpe);
+    double ddp = sf::div3(-d.dp[e] + dp_el);
     for (int i = 0; i < 3; ++i) d.stress[i * E + e] += ddp;
 }
 
@@ -632,7 +633,7 @@ __device__ __forceinline__ void force_elem_body(const Dev &d, int e, int4 c, con
     if (K.gravity != 0) {
         double Tn[4];
         load_nodal4(d.T, c, Tn);
-        buoy = mat_rho(K.M, K.M.mix[d.mix[e]], elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3])) * K.gravity / 4;
+        buoy = sf::quarter(mat_rho(K.M, K.M.mix[d.mix[e]], elem_mean4(Tn[0], Tn[1], Tn[2], Tn[3])) * K.gravity);
     }
     // (products on the integer pipes, sf::mul)
     for (int i = 0; i < 4; ++i) {
@@ -1080,9 +1081,9 @@ __global__ void k_fe_b_t(Dev d, int e0)
         int4 c = d.conn[e];
         double a[4];
         load_nodal4(d.ntmp, c, a);
-        double dj = 0;
-        for (int i = 0; i < 4; ++i) dj += a[i];
-        double edv = dj / 4;
+        double dj = sf::add0(a[0]);            // 0 + a0, then the rest; / 4
+        for (int i = 1; i < 4; ++i) dj += a[i];
+        double edv = sf::quarter(dj);
         d.edvoldt[e] = edv;
         double s[6], es[6], edot[6];
         load6(d.stress, E, e, s);
@@ -1142,10 +1143,10 @@ __global__ void k_fe_c(Dev d)
     int4 c = d.conn[e];
     double a[4];
     load_nodal4(d.ntmp, c, a);
-    double dpe = 0;
-    for (int i = 0; i < 4; ++i) dpe += a[i];
-    double dp_el = dpe / 4;
-    double ddp = (-d.dp[e] + dp_el) / 3;
+    double dpe = sf::add0(a[0]);                // 0 + a0, then the rest; / 4, / 3
+    for (int i = 1; i < 4; ++i) dpe += a[i];
+    double dp_el = sf::quarter(dpe);
+    double ddp = sf::div3(-d.dp[e] + dp_el);
     double s[6];
     load6(d.stress, E, e, s);
     for (int i = 0; i < 3; ++i) s[i] += ddp;
@@ -1209,6 +1210,12 @@ __global__ void k_fe_a(Dev d, int e0, unsigned nblocks)
         double dx[4], dy[4], dz[4];
         shape_fn(X, vol, dx, dy, dz);
         store_shp(d, e, dx, dy, dz);
+        // the element's dt candidates here, so that the coordinates are dead
+        // before the rotation's registers are needed (geometry.cxx:280-300)
+        if (dt_step) {
+            minh = min_height(X, vol);
+            dtd = 0.5 * minh * minh / K.therm_diff_max;
+        }
         const Mix &x = K.M.mix[d.mix[e]];
         {
             double Tn[4];
@@ -1233,10 +1240,6 @@ __global__ void k_fe_a(Dev d, int e0, unsigned nblocks)
             store6(d.strain, E, e, s);
         }
         next_step_contrib_d(d, e, c, D, dx, dy, dz, vol);
-        if (dt_step) {
-            minh = min_height(X, vol);
-            dtd = 0.5 * minh * minh / K.therm_diff_max;
-        }
     }
     if (dt_step) dt_reduce_and_finalize(d, minh, dtd, live, nblocks);
 }

@@ -204,6 +204,100 @@ DES_SF_HD double mul(double x, double y)
     return from_bits(mul_slow(a, b));
 }
 
+// 0.0 + x as the FP64 unit rounds it: x itself, except that -0.0 gives
+// +0.0 (a NaN comes back unchanged).  The first addition of a sum that
+// starts from zero.
+DES_SF_HD double add0(double x)
+{
+    const uint64_t b = bits(x);
+    return from_bits(b == kSign ? 0ull : b);
+}
+
+// 2 x and x / 2 (x * 2.0, x * 0.5) as the FP64 unit rounds them: an exponent
+// step where the operand and the result are normal, the integer multiply
+// otherwise (zeros, subnormals, infinities, NaN, overflow, a subnormal half)
+DES_SF_HD double twice(double x)
+{
+    const uint64_t b = bits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7ff;
+    if (e - 1 < 2045u) return from_bits(b + (1ull << 52));
+    return mul(x, 2.0);
+}
+
+DES_SF_HD double half(double x)
+{
+    const uint64_t b = bits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7ff;
+    if (e - 2 < 2045u) return from_bits(b - (1ull << 52));
+    return mul(x, 0.5);
+}
+
+// x / 4 (x * 0.25) as the FP64 unit rounds it
+DES_SF_HD double quarter(double x)
+{
+    const uint64_t b = bits(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7ff;
+    if (e - 3 < 2044u) return from_bits(b - (2ull << 52));
+    return mul(x, 0.25);
+}
+
+// x / (3 2^k), k = 0 or 1, for the cases the fast path of div3k leaves:
+// zeros, subnormals, operands whose quotient is subnormal, infinities, NaN
+#if defined(__CUDACC__)
+static __host__ __device__ __noinline__
+#else
+static
+#endif
+uint64_t div3k_slow(uint64_t a, int k)
+{
+    const uint64_t sign = a & kSign, ma = a & kAbs;
+    int ea = (int)(ma >> 52);
+    if (ea == 2047) return ma > kInf ? (a | kQuiet) : a;
+    if (ma == 0) return sign;
+    uint64_t m = (ma & kFrac) | (ea ? kHidden : 0);
+    if (!ea) {                           // normalise a subnormal significand to bit 52
+        const int s = clz64(m) - 11;
+        m <<= s;
+        ea = 1 - s;
+    }
+    const uint64_t M = m << 11, q = M / 3, r = M - 3 * q;
+    const int t = (int)(q >> 62);        // the quotient's top bit is bit 61 + t
+    const uint64_t rr = (q << (2 - t)) | (uint64_t)(r != 0);
+    int e = ea - 2 - k + t;
+    if (e < 1) {
+        const uint32_t sh = (uint32_t)(1 - e) > 63u ? 63u : (uint32_t)(1 - e);
+        uint64_t rs = rr >> sh;
+        rs |= (uint64_t)((rs << sh) != rr);
+        return round_pack(sign, 1, rs);
+    }
+    return round_pack(sign, e, rr);
+}
+
+// x / 3 (k = 0) and x / 6 (k = 1) as the FP64 unit's division rounds them.
+// With the significand m (2^52 <= m < 2^53), the quotient of M = m 2^11 by 3
+// (an integer division by a constant: a high multiply) holds 62 or 63 bits;
+// its top 53 are the result's significand, and the bits below them with the
+// remainder of the division (sticky) decide the rounding to nearest even.
+template <int k>
+DES_SF_HD double div3k(double x)
+{
+    const uint64_t a = bits(x);
+    const uint32_t e = (uint32_t)(a >> 52) & 0x7ff;
+    if (e - (3 + k) < 2044u - k) {       // the quotient is normal
+        const uint64_t M = ((a & kFrac) | kHidden) << 11;
+        const uint64_t q = M / 3, r = M - 3 * q;
+        const uint32_t t = (uint32_t)(q >> 62);
+        const uint32_t sh = 9 + t;
+        const uint64_t sig = q >> sh, rem = q & ((1ull << sh) - 1), hf = 1ull << (sh - 1);
+        const uint64_t up = (uint64_t)((rem > hf) | ((rem == hf) & ((r != 0) | (uint32_t)(sig & 1))));
+        return from_bits(((((uint64_t)(e - 3 - k + t)) << 52) + sig + up) | (a & kSign));
+    }
+    return from_bits(div3k_slow(a, k));
+}
+
+DES_SF_HD double div3(double x) { return div3k<0>(x); }
+DES_SF_HD double div6(double x) { return div3k<1>(x); }
+
 // the cases the fast path of to_float leaves: zeros, subnormal FP32
 // results, infinities, NaN, overflow
 #if defined(__CUDACC__)

@@ -9,6 +9,7 @@
 //   support         mesh.cxx:1703-1717  ascending element id per node
 // The facet search uses a sorted key table instead of the O(nseg*nelem) scan.
 #include "des_gpu.h"
+#include "des_topology.h"
 
 #include <algorithm>
 #include <cmath>
@@ -66,6 +67,11 @@ extern "C" void des_topology_free(des_topology *t)
 
 extern "C" int des_topology_build(const des_mesh_view *m, des_topology **out)
 {
+    return des::topology_build(m, out, true);
+}
+
+int des::topology_build(const des_mesh_view *m, des_topology **out, bool support)
+{
     if (!m || !out || m->nnode < 1 || m->nelem < 1 || !m->connectivity) return DES_ERR_ARG;
     if (m->nseg > 0 && (!m->segment || !m->segflag)) return DES_ERR_ARG;
     const int nn = m->nnode, ne = m->nelem;
@@ -79,10 +85,12 @@ extern "C" int des_topology_build(const des_mesh_view *m, des_topology **out)
     t->nnode = nn;
     t->nelem = ne;
     t->bcflag = alloc_array<unsigned>(nn);
-    t->support_offsets = alloc_array<int>((size_t)nn + 1);
-    t->support_elems = alloc_array<int>(4 * (size_t)ne);
-    t->support_slots = alloc_array<int>(4 * (size_t)ne);
-    if (!t->bcflag || !t->support_offsets || !t->support_elems || !t->support_slots) {
+    if (support) {
+        t->support_offsets = alloc_array<int>((size_t)nn + 1);
+        t->support_elems = alloc_array<int>(4 * (size_t)ne);
+        t->support_slots = alloc_array<int>(4 * (size_t)ne);
+    }
+    if (!t->bcflag || (support && (!t->support_offsets || !t->support_elems || !t->support_slots))) {
         des_topology_free(t);
         return DES_ERR_NOMEM;
     }
@@ -162,6 +170,10 @@ extern "C" int des_topology_build(const des_mesh_view *m, des_topology **out)
         }
     }
 
+    if (!support) {
+        *out = t;
+        return DES_OK;
+    }
     // support lists as CSR, elements ascending within each node
     std::vector<int> count(nn, 0);
     for (long long q = 0; q < 4LL * ne; ++q) ++count[m->connectivity[q]];

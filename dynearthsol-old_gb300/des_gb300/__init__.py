@@ -59,6 +59,7 @@ def lib():
     for f in FUNCTIONS:
         getattr(L, "des_gpu_" + f).argtypes = [C.c_void_p]
     L.des_gpu_compute_dt.argtypes = [C.c_void_p, P(C.c_double)]
+    L.des_gpu_download_support.argtypes = [C.c_void_p, P(C.c_int), P(C.c_int), P(C.c_int)]
     L.des_gpu_error_string.argtypes = [C.c_int]
     L.des_gpu_error_string.restype = C.c_char_p
     L.des_gpu_device_bytes.argtypes = [C.c_void_p]
@@ -233,6 +234,16 @@ class Device:
                                       capacity, C.byref(n)), "des_gpu_log_returns")
         return rec[:min(n.value, capacity)], n.value
 
+    def support(self):
+        """The device's support lists: (offsets, elements, slots) as des_topology holds them."""
+        N, E = self.mesh.nnode, self.mesh.nelem
+        off = np.zeros(N + 1, np.int32)
+        el = np.zeros(4 * E, np.int32)
+        sl = np.zeros(4 * E, np.int32)
+        _ck(self.L.des_gpu_download_support(self.h, abi.iptr(off), abi.iptr(el), abi.iptr(sl)),
+            "des_gpu_download_support")
+        return off, el, sl
+
     def bad_mesh_quality(self, check):
         """(code, index, cube root of the worst quality) of bad_mesh_quality."""
         code, index, q = C.c_int(), C.c_int(-1), C.c_double()
@@ -323,11 +334,11 @@ def write_checkpoint(path, mesh, state, compensation_pressure):
 
 
 def softf64_check(n, seed=20261203, device=0):
-    """Mismatches of the integer-pipe FP64 multiply and FP64 -> FP32
-    conversion against the device's FP64 unit over n seeded operands per
-    kind: [multiply, any bits; multiply, near 1; conversion, any bits;
-    conversion, FP32 range]."""
-    out = (C.c_ulonglong * 4)()
+    """Mismatches of the integer-pipe FP64 arithmetic against the device's
+    FP64 unit over n seeded operands per kind: [multiply, any bits; multiply,
+    near 1; conversion to FP32, any bits; conversion, FP32 range; 0 + x;
+    2 x; x / 2; x / 6; x / 3; x / 4]."""
+    out = (C.c_ulonglong * 10)()
     _ck(lib().des_gpu_softf64_check(device, n, seed, out), "des_gpu_softf64_check")
     return list(out)
 

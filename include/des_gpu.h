@@ -209,12 +209,20 @@ int  des_boundary_normals(const des_topology *topo, const int *connectivity,
 /* ---- device handle ---------------------------------------------------- */
 
 /* Allocates the device state for one mesh (replaces allocate_variables,
- * fields.cxx:13-54) and uploads connectivity, support lists and material
- * tables.  device < 0 keeps the current device. */
+ * fields.cxx:13-54), uploads connectivity, boundary flags and material
+ * tables and builds the support lists on the device (create_support,
+ * mesh.cxx:1703-1717; the same lists as des_topology_build's).  device < 0
+ * keeps the current device. */
 int  des_gpu_create(const des_mesh_view *mesh, const des_params *params, int device,
                     des_gpu **out);
 int  des_gpu_destroy(des_gpu *g);
 int  des_gpu_set_params(des_gpu *g, const des_params *params);
+
+/* The device's support lists (create_support, mesh.cxx:1703-1717), which
+ * des_gpu_create and des_gpu_remesh build on the device from the
+ * connectivity, copied into host arrays in des_topology's layout:
+ * offsets[nnode+1], elems[4*nelem], slots[4*nelem].  Synchronises. */
+int  des_gpu_download_support(des_gpu *g, int *offsets, int *elems, int *slots);
 
 /* New per-element marker counts [nelem][nmat] (mesh->elemmarkers layout) for
  * the same mesh: the device's material tables follow the counts that
@@ -492,14 +500,15 @@ const char *des_gpu_error_string(int code);
 long long   des_gpu_device_bytes(const des_gpu *g);
 /* number of kernels one des_gpu_step launches per step */
 int         des_gpu_kernels_per_step(const des_gpu *g);
-/* Self-check of the integer-pipe FP64 multiply and FP64 -> FP32 conversion
- * that the step kernels use in place of FP64 unit instructions (no reference
- * counterpart): n seeded pseudo-random operands per kind on `device`,
- * compared bit for bit with the device's own FP64 instructions.
- * mismatches[0..3]: multiply on any bit patterns, multiply on operands near
- * 1, conversion on any bit patterns, conversion within the FP32 range. */
+/* Self-check of the integer-pipe FP64 arithmetic that the step kernels use
+ * in place of FP64 unit instructions (no reference counterpart): n seeded
+ * pseudo-random operands per kind on `device`, compared bit for bit with the
+ * device's own FP64 instructions.  mismatches[0..9]: multiply on any bit
+ * patterns, multiply on operands near 1, conversion to FP32 on any bit
+ * patterns, conversion within the FP32 range, 0 + x, 2 x, x / 2, x / 6,
+ * x / 3, x / 4 (the last six on any bit patterns and on exponents 0-8). */
 int         des_gpu_softf64_check(int device, long long n, unsigned long long seed,
-                                  unsigned long long mismatches[4]);
+                                  unsigned long long mismatches[10]);
 
 #ifdef __cplusplus
 }

@@ -1,5 +1,6 @@
-// Host check of the integer FP64 multiply and FP64 -> FP32 conversion
-// (dynearthsol-old_gb300/csrc/des_softf64.cuh) against the host's IEEE
+// Host check of the integer FP64 multiply, FP64 -> FP32 conversion, 0 + x,
+// 2 x, x / 2, x / 6, x / 3 and x / 4 (dynearthsol-old_gb300/csrc/des_softf64.cuh)
+// against the host's IEEE
 // arithmetic, bit for bit, on seeded pseudo-random operands of several kinds.
 //   softf64_check <pairs per kind>   -> one line per kind; exit 1 on a mismatch
 #include "des_softf64.cuh"
@@ -86,6 +87,21 @@ static double single(int kind, uint64_t &s)
     }
 }
 
+// operands of the one-operand helpers: 0 any bits; 1 exponents near 1023; 2
+// exponents 0-8 (subnormals, results near the subnormal range); 3 exponents
+// 2038-2047 (overflow, infinities, NaN); 4 short significands (ties)
+static double unary(int kind, uint64_t &s)
+{
+    const uint64_t r1 = splitmix(s), r3 = splitmix(s);
+    switch (kind) {
+    case 0: return from_bits(r1);
+    case 1: return mk(r1 >> 63, 1013 + r3 % 21, r1);
+    case 2: return mk(r1 >> 63, r3 % 9, (r3 & 32) ? r1 : (r1 >> (r3 % 52)));
+    case 3: return mk(r1 >> 63, 2038 + r3 % 10, (r3 & 64) ? r1 : 0);
+    default: return mk(r1 >> 63, 1 + r3 % 2046, r1 & ~((1ull << (30 + r3 % 22)) - 1));
+    }
+}
+
 static bool same(double a, double b) { return bits(a) == bits(b) || (std::isnan(a) && std::isnan(b)); }
 
 static bool same_f(float a, float b)
@@ -137,5 +153,32 @@ int main(int argc, char **argv)
         printf("to_float kind %d: %lld values, %lld mismatches\n", kind, per, bad.load());
         total_bad += bad;
     }
+    const char *names[6] = {"add0", "twice", "half", "div6", "div3", "quarter"};
+    for (int op = 0; op < 6; ++op)
+        for (int kind = 0; kind < 5; ++kind) {
+            std::atomic<long long> bad{0};
+            std::vector<std::thread> th;
+            for (unsigned t = 0; t < nt; ++t)
+                th.emplace_back([&, t] {
+                    uint64_t s = 0xadd06000ull + 1000003ull * (5 * op + kind) + 7919ull * t;
+                    for (long long i = t; i < per; i += nt) {
+                        const double x = unary(kind, s);
+                        volatile double vx = x;
+                        double h, g;
+                        switch (op) {
+                        case 0: h = 0.0 + vx; g = des::sf::add0(x); break;
+                        case 1: h = vx * 2.0; g = des::sf::twice(x); break;
+                        case 2: h = vx * 0.5; g = des::sf::half(x); break;
+                        case 3: h = vx / 6.0; g = des::sf::div6(x); break;
+                        case 4: h = vx / 3.0; g = des::sf::div3(x); break;
+                        default: h = vx * 0.25; g = des::sf::quarter(x); break;
+                        }
+                        if (!same(h, g) && bad++ < 3) printf("%s %a: host %a, integer %a\n", names[op], x, h, g);
+                    }
+                });
+            for (auto &x : th) x.join();
+            printf("%s kind %d: %lld values, %lld mismatches\n", names[op], kind, per, bad.load());
+            total_bad += bad;
+        }
     return total_bad ? 1 : 0;
 }

@@ -121,3 +121,43 @@ def test_remesh_keeps_closure_and_averaging():
     avg = dev.download_averages(5)        # sized for the new mesh
     assert avg.interval == 5 and avg.time0 > 0
     dev.close()
+
+
+def assert_support_equal(dev, mesh, oracle=None):
+    topo = D.Topology(mesh)                   # des_topology_build on the host
+    off, el, sl = dev.support()
+    assert np.array_equal(off, topo.support_offsets)
+    assert np.array_equal(el, topo.support_elems)
+    assert np.array_equal(sl, topo.support_slots)
+    if oracle is not None:                    # create_support as the oracle restates it
+        o_off, o_el = oracle.support()
+        assert np.array_equal(off, o_off) and np.array_equal(el, o_el)
+
+
+def test_support_lists_built_on_the_device_after_create_and_remesh():
+    """create_support (mesh.cxx:1703-1717) on the device, in des_gpu_create and
+    again in des_gpu_remesh for the new mesh (remeshing.cxx:2011-2012): the
+    same CSR, element for element, as the host build and the oracle's."""
+    cfg = phase_config()
+    c = Case(cfg)
+    dev = fresh_device(c, c.params)
+    assert_support_equal(dev, c.mesh, c.oracle)
+    want = c.initial_state()
+    c.oracle.step(want, 5)
+    dev.step(5)
+    mesh2, s = remesh_standin(c.mesh, want, c.mesh.elemmarkers, new_cfg(cfg, 11, 8, 6))
+    dev.remesh(mesh2, s, reset_bottom_coord0=True)
+    assert_support_equal(dev, mesh2, new_oracle(c, mesh2))
+    dev.close()
+
+
+def test_support_lists_on_the_device_config2_size():
+    """The same on config 2's mesh (9.6M tets, 1.66M nodes: 1,618 scan blocks)."""
+    c = W.CONFIGS["2"]
+    mesh, p, T, pls, topo = D.setup_case(c)
+    dev = D.Device(mesh, p, device=0)
+    off, el, sl = dev.support()
+    dev.close()
+    assert np.array_equal(off, topo.support_offsets)
+    assert np.array_equal(el, topo.support_elems)
+    assert np.array_equal(sl, topo.support_slots)
