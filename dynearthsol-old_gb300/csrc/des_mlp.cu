@@ -1,16 +1,14 @@
 // Training and standalone evaluation of the learned return-map closure
 // (see des_mlp.cuh for the network).  Forward and backward passes run on the
-// tensor cores (BF16 operands, FP32 accumulation); Adam keeps FP32 master
-// weights and moments and writes the BF16 copies the MMAs read.
-//
-// Per CTA: one tile of 64 samples (4 warps x 16 rows).  Backward GEMMs:
-//   dW3 = dY^T H2, dH2 = (dY W3) * [H2 > 0], dW2 = dH2^T H1,
-//   dH1 = (dH2 W2) * [H1 > 0], dW1 = dH1^T X, biases = column sums;
-// every partial gradient of the tile is added to the global FP32 gradient
-// with atomics (one add per parameter per tile).
+// fifth-generation tensor cores (des_mlp_tc.cuh: tcgen05 MMAs, BF16 operands
+// in shared memory, FP32 accumulators in tensor memory), one CTA per tile of
+// 128 samples; each tile's gradient is added to the global FP32 gradient with
+// atomics (one add per parameter per tile).  Adam keeps FP32 master weights
+// and moments.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -18,195 +16,48 @@
 
 #include "des_gpu.h"
 #include "des_mlp.cuh"
+#include "des_mlp_tc.cuh"
 
 using namespace des;
 
 namespace {
 
-constexpr int kTile = 64;                    // samples per CTA
+constexpr int kTile = kTcRows;               // samples per CTA
 constexpr int kNW1 = kMlpHid * kMlpIn, kNW2 = kMlpHid * kMlpHid, kNW3 = kMlpOut * kMlpHid;
 constexpr int kNParams = kNW1 + kMlpHid + kNW2 + kMlpHid + kNW3 + kMlpOut;   // 5,768
 // offsets of the parameter groups in a flat FP32 vector
 constexpr int kOW1 = 0, kOB1 = kOW1 + kNW1, kOW2 = kOB1 + kMlpHid, kOB2 = kOW2 + kNW2,
               kOW3 = kOB2 + kMlpHid, kOB3 = kOW3 + kNW3;
+static_assert(kOB1 == mlptc::oB1 && kOW2 == mlptc::oW2 && kOB2 == mlptc::oB2 && kOW3 == mlptc::oW3 &&
+                  kOB3 == mlptc::oB3,
+              "parameter layout");
 
-struct TrainSmem {
-    __nv_bfloat16 x[kTile * kMlpIn];
-    __nv_bfloat16 h1[kTile * kHStride], h2[kTile * kHStride];
-    __nv_bfloat16 dh1[kTile * kHStride], dh2[kTile * kHStride];
-    __nv_bfloat16 dy[kTile * 16];
-    float y[kTile * kMlpOut];
-    __nv_bfloat16 w1[kNW1], w2[kNW2], w3p[16 * kMlpHid];
-    float b1[kMlpHid], b2[kMlpHid], b3[kMlpOut];
-};
-
-// flat FP32 parameters -> the BF16/FP32 arrays a CTA keeps in shared memory
-__device__ void load_params(TrainSmem &S, const float *P)
+__device__ __forceinline__ MlpTcSmem &tc_smem(unsigned char *raw)
 {
-    for (int i = threadIdx.x; i < kNW1; i += blockDim.x) S.w1[i] = __float2bfloat16(P[kOW1 + i]);
-    for (int i = threadIdx.x; i < kNW2; i += blockDim.x) S.w2[i] = __float2bfloat16(P[kOW2 + i]);
-    for (int i = threadIdx.x; i < 16 * kMlpHid; i += blockDim.x)
-        S.w3p[i] = __float2bfloat16(i < kNW3 ? P[kOW3 + i] : 0.f);
-    for (int i = threadIdx.x; i < kMlpHid; i += blockDim.x) {
-        S.b1[i] = P[kOB1 + i];
-        S.b2[i] = P[kOB2 + i];
-    }
-    for (int i = threadIdx.x; i < kMlpOut; i += blockDim.x) S.b3[i] = P[kOB3 + i];
+    return *reinterpret_cast<MlpTcSmem *>((reinterpret_cast<uintptr_t>(raw) + 1023) & ~uintptr_t(1023));
 }
 
-// loads rows [row0, row0 + 64) of x (FP32 [n][16]) as bf16, zero rows past n
-__device__ void load_x(TrainSmem &S, const float *x, long long n, long long row0)
+__global__ void __launch_bounds__(kTcRows) k_mlp_forward(const float *P, const float *x, long long n, float *y,
+                                                         int *err)
 {
-    for (int i = threadIdx.x; i < kTile * kMlpIn; i += blockDim.x) {
-        long long r = row0 + i / kMlpIn;
-        S.x[i] = __float2bfloat16(r < n ? x[r * kMlpIn + (i % kMlpIn)] : 0.f);
-    }
-}
-
-__global__ void __launch_bounds__(128) k_mlp_forward(const float *P, const float *x, long long n, float *y)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TrainSmem &S = *reinterpret_cast<TrainSmem *>(smem_raw);
-    const long long row0 = (long long)blockIdx.x * kTile;
-    load_params(S, P);
-    load_x(S, x, n, row0);
-    __syncthreads();
-    const int w = threadIdx.x >> 5;
-    mlp_forward16(S.x + w * 16 * kMlpIn, S.w1, S.w2, S.w3p, S.b1, S.b2, S.b3, S.h1 + w * 16 * kHStride,
-                  S.h2 + w * 16 * kHStride, S.y + w * 16 * kMlpOut);
-    __syncthreads();
-    for (int i = threadIdx.x; i < kTile * kMlpOut; i += blockDim.x) {
-        long long r = row0 + i / kMlpOut;
-        if (r < n) y[r * kMlpOut + (i % kMlpOut)] = S.y[i];
-    }
-}
-
-// accumulator fragment -> atomic adds into a [rows][cols] FP32 gradient
-__device__ __forceinline__ void atomic_frag(float *G, int ldg, int r0, int n0, const float d[4], int rmax)
-{
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int c = n0 + 2 * t;
-    if (r0 + g < rmax) {
-        atomicAdd(G + (r0 + g) * ldg + c, d[0]);
-        atomicAdd(G + (r0 + g) * ldg + c + 1, d[1]);
-    }
-    if (r0 + g + 8 < rmax) {
-        atomicAdd(G + (r0 + g + 8) * ldg + c, d[2]);
-        atomicAdd(G + (r0 + g + 8) * ldg + c + 1, d[3]);
-    }
-}
-
-// masked store of a fragment into a bf16 [rows][kHStride] tile: value * [H > 0]
-__device__ __forceinline__ void store_masked(__nv_bfloat16 *D, const __nv_bfloat16 *H, int r0, int n0,
-                                             const float d[4])
-{
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    const int c = n0 + 2 * t;
-    const int i0 = (r0 + g) * kHStride + c, i1 = (r0 + g + 8) * kHStride + c;
-    float m0 = __bfloat162float(H[i0]) > 0.f ? 1.f : 0.f, m1 = __bfloat162float(H[i0 + 1]) > 0.f ? 1.f : 0.f;
-    float m2 = __bfloat162float(H[i1]) > 0.f ? 1.f : 0.f, m3 = __bfloat162float(H[i1 + 1]) > 0.f ? 1.f : 0.f;
-    *reinterpret_cast<uint32_t *>(D + i0) = pack_bf16(d[0] * m0, d[1] * m1);
-    *reinterpret_cast<uint32_t *>(D + i1) = pack_bf16(d[2] * m2, d[3] * m3);
+    extern __shared__ unsigned char smem_raw[];
+    MlpTcSmem &S = tc_smem(smem_raw);
+    const bool ok = mlptc_tile<false>(S, P, x, nullptr, n, (long long)blockIdx.x * kTile, 0.f, y, nullptr,
+                                      nullptr);
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
 }
 
 // one tile: forward, loss, backward; grad += d(loss)/d(params) where loss is
 // the mean over `count` samples of the summed squared error of the 7 outputs
-__global__ void __launch_bounds__(128) k_mlp_grad(const float *P, const float *x, const float *yt,
-                                                  long long n, long long row_begin, float inv_count,
-                                                  float *grad, double *loss)
+__global__ void __launch_bounds__(kTcRows) k_mlp_grad(const float *P, const float *x, const float *yt,
+                                                      long long n, long long row_begin, float inv_count,
+                                                      float *grad, double *loss, int *err)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    TrainSmem &S = *reinterpret_cast<TrainSmem *>(smem_raw);
-    const long long row0 = row_begin + (long long)blockIdx.x * kTile;
-    const int w = threadIdx.x >> 5;
-    load_params(S, P);
-    load_x(S, x, n, row0);
-    __syncthreads();
-    mlp_forward16(S.x + w * 16 * kMlpIn, S.w1, S.w2, S.w3p, S.b1, S.b2, S.b3, S.h1 + w * 16 * kHStride,
-                  S.h2 + w * 16 * kHStride, S.y + w * 16 * kMlpOut);
-    __syncthreads();
-    // dY and the loss of this tile
-    double l = 0.0;
-    for (int i = threadIdx.x; i < kTile * 16; i += blockDim.x) {
-        int r = i / 16, j = i % 16;
-        long long gr = row0 + r;
-        float dv = 0.f;
-        if (j < kMlpOutUsed && gr < n) {
-            float e = S.y[r * kMlpOut + j] - yt[gr * kMlpOut + j];
-            l += (double)e * e;
-            dv = 2.f * e * inv_count;
-        }
-        S.dy[i] = __float2bfloat16(dv);
-    }
-    for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(loss, l * inv_count);
-    __syncthreads();
-    uint32_t a[4], b[2];
-    // dW3 [8 x 64] (M padded to 16): A(j, r) = dY[r][j], B(r, c) = H2[r][c]
-    for (int nt = w * 2; nt < w * 2 + 2; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kTile / 16; ++kt) {
-            frag_a_gen(a, S.dy, 1, 16, 0, kt * 16);
-            frag_b_gen(b, S.h2, kHStride, 1, kt * 16, nt * 8);
-            mma_bf16(d, a, b);
-        }
-        atomic_frag(grad + kOW3, kMlpHid, 0, nt * 8, d, kMlpOutUsed);
-    }
-    // dH2 = dY W3 * [H2 > 0], rows of this warp: A = dY rows, B(j, c) = W3[j][c]
-    for (int nt = 0; nt < kMlpHid / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        frag_a_row(a, S.dy, 16, w * 16, 0);
-        frag_b_gen(b, S.w3p, kMlpHid, 1, 0, nt * 8);
-        mma_bf16(d, a, b);
-        store_masked(S.dh2, S.h2, w * 16, nt * 8, d);
-    }
-    __syncthreads();
-    // dW2 [64 x 64]: A(o, r) = dH2[r][o], B(r, i) = H1[r][i]; warp w owns rows o in [16w, 16w+16)
-    for (int nt = 0; nt < kMlpHid / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kTile / 16; ++kt) {
-            frag_a_gen(a, S.dh2, 1, kHStride, w * 16, kt * 16);
-            frag_b_gen(b, S.h1, kHStride, 1, kt * 16, nt * 8);
-            mma_bf16(d, a, b);
-        }
-        atomic_frag(grad + kOW2, kMlpHid, w * 16, nt * 8, d, kMlpHid);
-    }
-    // dH1 = dH2 W2 * [H1 > 0]: A = dH2 rows of this warp, B(o, i) = W2[o][i]
-    for (int nt = 0; nt < kMlpHid / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kMlpHid / 16; ++kt) {
-            frag_a_row(a, S.dh2, kHStride, w * 16, kt * 16);
-            frag_b_gen(b, S.w2, kMlpHid, 1, kt * 16, nt * 8);
-            mma_bf16(d, a, b);
-        }
-        store_masked(S.dh1, S.h1, w * 16, nt * 8, d);
-    }
-    __syncthreads();
-    // dW1 [64 x 16]: A(o, r) = dH1[r][o], B(r, i) = X[r][i]
-    for (int nt = 0; nt < kMlpIn / 8; ++nt) {
-        float d[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int kt = 0; kt < kTile / 16; ++kt) {
-            frag_a_gen(a, S.dh1, 1, kHStride, w * 16, kt * 16);
-            frag_b_gen(b, S.x, kMlpIn, 1, kt * 16, nt * 8);
-            mma_bf16(d, a, b);
-        }
-        atomic_frag(grad + kOW1, kMlpIn, w * 16, nt * 8, d, kMlpHid);
-    }
-    // bias gradients: column sums of dY, dH2, dH1 (bf16 values, as the MMAs use)
-    for (int c = threadIdx.x; c < kMlpHid; c += blockDim.x) {
-        float s1 = 0.f, s2 = 0.f;
-        for (int r = 0; r < kTile; ++r) {
-            s1 += __bfloat162float(S.dh1[r * kHStride + c]);
-            s2 += __bfloat162float(S.dh2[r * kHStride + c]);
-        }
-        atomicAdd(grad + kOB1 + c, s1);
-        atomicAdd(grad + kOB2 + c, s2);
-    }
-    for (int j = threadIdx.x; j < kMlpOutUsed; j += blockDim.x) {
-        float s3 = 0.f;
-        for (int r = 0; r < kTile; ++r) s3 += __bfloat162float(S.dy[r * 16 + j]);
-        atomicAdd(grad + kOB3 + j, s3);
-    }
+    extern __shared__ unsigned char smem_raw[];
+    MlpTcSmem &S = tc_smem(smem_raw);
+    const bool ok = mlptc_tile<true>(S, P, x, yt, n, row_begin + (long long)blockIdx.x * kTile, inv_count,
+                                     nullptr, grad, loss);
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
 }
 
 // Adam (Kingma & Ba 2015) on the flat FP32 parameters; padded entries stay 0
@@ -257,10 +108,18 @@ struct DevBuf {
 
 int smem_setup(const void *fn)
 {
-    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TrainSmem)) ==
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpTcSmemBytes) ==
                    cudaSuccess
                ? DES_OK
                : DES_ERR_CUDA;
+}
+
+// the kernels' time-out flag: DES_ERR_CUDA when a tensor-core wait gave up
+int read_err(const int *derr)
+{
+    int e = 0;
+    if (cudaMemcpy(&e, derr, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return DES_ERR_CUDA;
+    return e ? DES_ERR_CUDA : DES_OK;
 }
 
 }  // namespace
@@ -272,17 +131,20 @@ int des_mlp_forward(const des_mlp *net, const float *x, long long n, float *y)
     if (!net || !x || !y || n < 1) return DES_ERR_ARG;
     std::vector<float> P;
     pack(*net, P);
-    DevBuf dP, dx, dy;
+    DevBuf dP, dx, dy, de;
     if (dP.alloc(sizeof(float) * kNParams) || dx.alloc(sizeof(float) * n * kMlpIn) ||
-        dy.alloc(sizeof(float) * n * kMlpOut))
+        dy.alloc(sizeof(float) * n * kMlpOut) || de.alloc(sizeof(int)))
         return DES_ERR_NOMEM;
     if (smem_setup((const void *)k_mlp_forward)) return DES_ERR_CUDA;
     if (cudaMemcpy(dP.p, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice) ||
-        cudaMemcpy(dx.p, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice))
+        cudaMemcpy(dx.p, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice) ||
+        cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
     int grid = (int)((n + kTile - 1) / kTile);
-    k_mlp_forward<<<grid, 128, sizeof(TrainSmem)>>>(dP.as<float>(), dx.as<float>(), n, dy.as<float>());
+    k_mlp_forward<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), n, dy.as<float>(),
+                                                      de.as<int>());
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return DES_ERR_CUDA;
+    if (int rc = read_err(de.as<int>())) return rc;
     return cudaMemcpy(y, dy.p, sizeof(float) * n * kMlpOut, cudaMemcpyDeviceToHost) == cudaSuccess ? DES_OK
                                                                                                     : DES_ERR_CUDA;
 }
@@ -293,20 +155,23 @@ int des_mlp_loss_grad(const des_mlp *net, const float *x, const float *y, long l
     if (!net || !x || !y || n < 1 || !loss || !grad) return DES_ERR_ARG;
     std::vector<float> P;
     pack(*net, P);
-    DevBuf dP, dx, dy, dg, dl;
+    DevBuf dP, dx, dy, dg, dl, de;
     if (dP.alloc(sizeof(float) * kNParams) || dx.alloc(sizeof(float) * n * kMlpIn) ||
-        dy.alloc(sizeof(float) * n * kMlpOut) || dg.alloc(sizeof(float) * kNParams) || dl.alloc(sizeof(double)))
+        dy.alloc(sizeof(float) * n * kMlpOut) || dg.alloc(sizeof(float) * kNParams) || dl.alloc(sizeof(double)) ||
+        de.alloc(sizeof(int)))
         return DES_ERR_NOMEM;
     if (smem_setup((const void *)k_mlp_grad)) return DES_ERR_CUDA;
     if (cudaMemcpy(dP.p, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice) ||
         cudaMemcpy(dx.p, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice) ||
         cudaMemcpy(dy.p, y, sizeof(float) * n * kMlpOut, cudaMemcpyHostToDevice) ||
-        cudaMemset(dg.p, 0, sizeof(float) * kNParams) || cudaMemset(dl.p, 0, sizeof(double)))
+        cudaMemset(dg.p, 0, sizeof(float) * kNParams) || cudaMemset(dl.p, 0, sizeof(double)) ||
+        cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
     int grid = (int)((n + kTile - 1) / kTile);
-    k_mlp_grad<<<grid, 128, sizeof(TrainSmem)>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n, 0,
-                                                 1.f / (float)n, dg.as<float>(), dl.as<double>());
+    k_mlp_grad<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n, 0,
+                                                   1.f / (float)n, dg.as<float>(), dl.as<double>(), de.as<int>());
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return DES_ERR_CUDA;
+    if (int rc = read_err(de.as<int>())) return rc;
     std::vector<float> G(kNParams);
     if (cudaMemcpy(G.data(), dg.p, sizeof(float) * kNParams, cudaMemcpyDeviceToHost) ||
         cudaMemcpy(loss, dl.p, sizeof(double), cudaMemcpyDeviceToHost))
@@ -333,18 +198,18 @@ int des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int
     }
     std::vector<float> P;
     pack(*net, P);
-    DevBuf dP, dx, dy, dg, dm, dv, dl;
+    DevBuf dP, dx, dy, dg, dm, dv, dl, de;
     if (dP.alloc(sizeof(float) * kNParams) || dx.alloc(sizeof(float) * n * kMlpIn) ||
         dy.alloc(sizeof(float) * n * kMlpOut) || dg.alloc(sizeof(float) * kNParams) ||
         dm.alloc(sizeof(float) * kNParams) || dv.alloc(sizeof(float) * kNParams) ||
-        dl.alloc(sizeof(double) * (size_t)steps))
+        dl.alloc(sizeof(double) * (size_t)steps) || de.alloc(sizeof(int)))
         return DES_ERR_NOMEM;
     if (smem_setup((const void *)k_mlp_grad)) return DES_ERR_CUDA;
     if (cudaMemcpy(dP.p, P.data(), sizeof(float) * kNParams, cudaMemcpyHostToDevice) ||
         cudaMemcpy(dx.p, xs.data(), sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice) ||
         cudaMemcpy(dy.p, ys.data(), sizeof(float) * n * kMlpOut, cudaMemcpyHostToDevice) ||
         cudaMemset(dm.p, 0, sizeof(float) * kNParams) || cudaMemset(dv.p, 0, sizeof(float) * kNParams) ||
-        cudaMemset(dl.p, 0, sizeof(double) * (size_t)steps))
+        cudaMemset(dl.p, 0, sizeof(double) * (size_t)steps) || cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
     const long long nb = n / batch;
     const int grid = batch / kTile;
@@ -353,13 +218,14 @@ int des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int
         // cosine decay of the step size from lr to lr / 100
         const float lr_s = lr * (0.01f + 0.99f * 0.5f * (1.f + cosf(3.14159265f * (float)s / (float)steps)));
         cudaMemsetAsync(dg.p, 0, sizeof(float) * kNParams);
-        k_mlp_grad<<<grid, 128, sizeof(TrainSmem)>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n,
-                                                     begin, 1.f / (float)batch, dg.as<float>(),
-                                                     dl.as<double>() + s);
+        k_mlp_grad<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n,
+                                                       begin, 1.f / (float)batch, dg.as<float>(),
+                                                       dl.as<double>() + s, de.as<int>());
         k_adam<<<(kNParams + 255) / 256, 256>>>(dP.as<float>(), dm.as<float>(), dv.as<float>(),
                                                dg.as<float>(), s + 1, lr_s);
     }
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return DES_ERR_CUDA;
+    if (int rc = read_err(de.as<int>())) return rc;
     if (cudaMemcpy(P.data(), dP.p, sizeof(float) * kNParams, cudaMemcpyDeviceToHost)) return DES_ERR_CUDA;
     unpack(P, *net);
     if (loss_trace) {

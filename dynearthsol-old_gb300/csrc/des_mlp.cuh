@@ -1,6 +1,10 @@
 // The learned return-map closure: a 14 -> 64 -> 64 -> 7 MLP with ReLU, BF16
-// weights and activations, FP32 accumulation, evaluated with warp-level
-// tensor-core MMAs (m16n8k16, BF16 x BF16 -> FP32).
+// weights and activations, FP32 accumulation.  Training and the standalone
+// forward pass run on tcgen05 MMAs with TMEM accumulators, 128 samples per
+// CTA (des_mlp_tc.cuh).  Inside the FP32 stress pass the network is evaluated
+// by one warp per 16 candidates with warp-level MMAs (m16n8k16, BF16 x BF16
+// -> FP32, below): there every warp works through its own share of the list of
+// undecided elements, and its tiles fill as candidates come.
 //
 // Shapes (inputs and outputs padded for the 16x16 / 16x8 MMA tiles):
 //   x  [rows][16]   14 normalised inputs + 2 zeros
