@@ -1189,8 +1189,11 @@ __global__ void k_fn_c(Dev d)
 
 // E-A: update_mesh element half, rotate_stress, next-step contributions, dt;
 // this launch covers the elements from e0 (a multiple of the block size), the
-// pass nblocks blocks in all
-__global__ void k_fe_a(Dev d, int e0, unsigned nblocks)
+// pass nblocks blocks in all.  Six blocks of 128 per SM (80 registers, a few
+// spilled): the pass waits on FP64 results and on instruction fetch more than
+// on any pipe, and the extra warps hide more of that (measured 5.16 against
+// 5.27 ms at five blocks on config 2)
+__global__ void __launch_bounds__(128, 6) k_fe_a(Dev d, int e0, unsigned nblocks)
 {
     int e = e0 + gtid();
     const Consts &K = *d.K;
