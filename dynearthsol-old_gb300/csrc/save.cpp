@@ -1,13 +1,15 @@
 // The .save file of one output frame, as Output::_write (output.cxx:73-198)
 // writes it through BinaryOutput (binaryio.cxx:44-131), from host arrays in
-// the reference's layout.  Marker sets are not written (has_marker_output
-// off).  Derived element fields (density, mesh quality, viscosity, material)
-// are computed here on the host with the reference's arithmetic and libm, so
-// the file matches the reference's byte for byte.
+// the reference's layout, and the .chkpt file (output.cxx:270-296), each with
+// the marker sets it is given.  Derived element fields (density, mesh
+// quality, viscosity, material) and marker coordinates are computed here on
+// the host with the reference's arithmetic and libm, so the files match the
+// reference's byte for byte.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "des_gpu.h"
@@ -145,10 +147,63 @@ double visc(const des_params &p, const int *markers, int nmat, const int *conn, 
     return std::min(std::max(v, p.visc_min), p.visc_max);
 }
 
+// checks one marker set against the mesh it refers to
+int check_set(const des_marker_set &ms, int nelem)
+{
+    if (!ms.name || ms.nmarkers < 0) return DES_ERR_ARG;
+    if (ms.nmarkers > 0 && (!ms.eta || !ms.elem || !ms.mattype || !ms.id)) return DES_ERR_ARG;
+    for (int i = 0; i < ms.nmarkers; ++i)
+        if (ms.elem[i] < 0 || ms.elem[i] >= nelem) return DES_ERR_ARG;
+    return DES_OK;
+}
+
+int check_sets(const des_marker_set *sets, int nsets, int nelem)
+{
+    if (nsets < 0 || (nsets > 0 && !sets)) return DES_ERR_ARG;
+    for (int k = 0; k < nsets; ++k)
+        if (int rc = check_set(sets[k], nelem)) return rc;
+    return DES_OK;
+}
+
+std::string field(const des_marker_set &ms, const char *suffix) { return std::string(ms.name) + suffix; }
+
+// MarkerSet::write_save_file (markerset.cxx:452-483): the markers' positions
+// x_j = sum_k eta_k x(conn_k)_j, in that order from zero
+void write_set_save(SaveFile &bin, const des_marker_set &ms, const int *conn, const double *coord)
+{
+    const int n = ms.nmarkers;
+    bin.write(&n, 1, field(ms, " size").c_str());
+    std::vector<double> mc(3 * (std::size_t)n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        const int *c = conn + 4 * (std::size_t)ms.elem[i];
+        const double *eta = ms.eta + 4 * (std::size_t)i;
+        double *x = mc.data() + 3 * (std::size_t)i;
+        for (int j = 0; j < 3; j++)
+            for (int k = 0; k < 4; k++) x[j] += eta[k] * coord[3 * (std::size_t)c[k] + j];
+    }
+    bin.write(mc.data(), 3 * (std::size_t)n, field(ms, ".coord").c_str());
+    bin.write(ms.elem, (std::size_t)n, field(ms, ".elem").c_str());
+    bin.write(ms.mattype, (std::size_t)n, field(ms, ".mattype").c_str());
+    bin.write(ms.id, (std::size_t)n, field(ms, ".id").c_str());
+}
+
+// MarkerSet::write_chkpt_file (markerset.cxx:407-419)
+void write_set_chkpt(SaveFile &bin, const des_marker_set &ms)
+{
+    const int n = ms.nmarkers;
+    const int size[2] = {n, ms.last_id};
+    bin.write(size, 2, field(ms, " size").c_str());
+    bin.write(ms.eta, 4 * (std::size_t)n, field(ms, ".eta").c_str());
+    bin.write(ms.elem, (std::size_t)n, field(ms, ".elem").c_str());
+    bin.write(ms.mattype, (std::size_t)n, field(ms, ".mattype").c_str());
+    bin.write(ms.id, (std::size_t)n, field(ms, ".id").c_str());
+}
+
 }  // namespace
 
 extern "C" int des_write_save(const char *path, const des_mesh_view *m, const des_params *p,
-                              const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg)
+                              const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg,
+                              const des_marker_set *sets, int nsets)
 {
     if (!path || !m || !p || !bcflag || !s || !m->connectivity || !m->elemmarkers) return DES_ERR_ARG;
     if (s->nnode != m->nnode || s->nelem != m->nelem) return DES_ERR_ARG;
@@ -157,6 +212,7 @@ extern "C" int des_write_save(const char *path, const des_mesh_view *m, const de
         return DES_ERR_ARG;
     if (avg && (!avg->coord0 || !avg->strain0 || !avg->stress_sum || !avg->dpls_sum || avg->interval < 1))
         return DES_ERR_ARG;
+    if (check_sets(sets, nsets, m->nelem)) return DES_ERR_ARG;
     const std::size_t N = m->nnode, E = m->nelem;
     const int *conn = m->connectivity;
     SaveFile bin(path);
@@ -209,16 +265,19 @@ extern "C" int des_write_save(const char *path, const des_mesh_view *m, const de
     bin.write(s->force, 3 * N, "force");
     bin.write(s->coord0, 3 * N, "coord0");
     bin.write(bcflag, N, "bcflag");
+    for (int k = 0; k < nsets; ++k) write_set_save(bin, sets[k], conn, s->coord);
     return bin.close();
 }
 
-// Output::write_checkpoint (output.cxx:270-296) for a model without marker
-// sets in 3D: time and compensation pressure, segments, segment flags and
-// volume_old.
+// Output::write_checkpoint (output.cxx:270-296) in 3D: time and
+// compensation pressure, segments, segment flags, volume_old, then the
+// marker sets.
 extern "C" int des_write_checkpoint(const char *path, const des_mesh_view *m, double time,
-                                    double compensation_pressure, const double *volume_old)
+                                    double compensation_pressure, const double *volume_old,
+                                    const des_marker_set *sets, int nsets)
 {
     if (!path || !m || !volume_old || (m->nseg > 0 && (!m->segment || !m->segflag))) return DES_ERR_ARG;
+    if (check_sets(sets, nsets, m->nelem)) return DES_ERR_ARG;
     SaveFile bin(path);
     if (!bin.ok()) return DES_ERR_ARG;
     const double tc[2] = {time, compensation_pressure};
@@ -226,5 +285,6 @@ extern "C" int des_write_checkpoint(const char *path, const des_mesh_view *m, do
     bin.write(m->segment, 3 * (std::size_t)m->nseg, "segment");
     bin.write(m->segflag, (std::size_t)m->nseg, "segflag");
     bin.write(volume_old, (std::size_t)m->nelem, "volume_old");
+    for (int k = 0; k < nsets; ++k) write_set_chkpt(bin, sets[k]);
     return bin.close();
 }

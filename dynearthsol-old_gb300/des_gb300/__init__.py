@@ -85,8 +85,9 @@ def lib():
                                            P(C.c_double)]
     L.des_gpu_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
     L.des_write_save.argtypes = [C.c_char_p, P(abi.MeshView), P(abi.Params), P(C.c_uint),
-                                 P(abi.StateView), P(abi.SaveAverages)]
-    L.des_write_checkpoint.argtypes = [C.c_char_p, P(abi.MeshView), C.c_double, C.c_double, P(C.c_double)]
+                                 P(abi.StateView), P(abi.SaveAverages), P(abi.MarkerSet), C.c_int]
+    L.des_write_checkpoint.argtypes = [C.c_char_p, P(abi.MeshView), C.c_double, C.c_double, P(C.c_double),
+                                       P(abi.MarkerSet), C.c_int]
     L.des_gpu_set_averaging.argtypes = [C.c_void_p, C.c_int]
     L.des_gpu_output_snapshot.argtypes = [C.c_void_p, C.c_uint]
     L.des_gpu_output_fetch.argtypes = [C.c_void_p, P(abi.StateView)]
@@ -317,20 +318,44 @@ def save_averages(coord0, strain0, stress_sum, dpls_sum, time0, interval):
     return a
 
 
-def write_save(path, mesh, params, bcflag, state, averages=None):
-    """The .save file of one output frame (des_write_save)."""
+def marker_sets(sets):
+    """A ctypes array of des_marker_set from (name, eta [n][4], elem, mattype,
+    id, last_id) tuples; the numpy arrays it points into ride along on it."""
+    if not sets:
+        return None, 0
+    arr = (abi.MarkerSet * len(sets))()
+    keep = []
+    for k, (name, eta, elem, mattype, ids, last_id) in enumerate(sets):
+        eta = np.ascontiguousarray(eta, dtype=np.float64).reshape(-1, 4)
+        cols = [np.ascontiguousarray(a, dtype=np.int32) for a in (elem, mattype, ids)]
+        if any(c.ndim != 1 or c.size != len(eta) for c in cols):
+            raise ValueError(f"marker set {name}: eta, elem, mattype and id differ in length")
+        keep += [eta] + cols
+        arr[k] = abi.MarkerSet(str(name).encode(), len(eta), int(last_id), abi.dptr(eta), abi.iptr(cols[0]),
+                               abi.iptr(cols[1]), abi.iptr(cols[2]))
+    arr._keep = keep
+    return arr, len(sets)
+
+
+def write_save(path, mesh, params, bcflag, state, averages=None, markers=None):
+    """The .save file of one output frame (des_write_save); markers: marker
+    sets as (name, eta, elem, mattype, id, last_id), written as with
+    sim.has_marker_output on."""
     v = state.view()
     mv = mesh.view()
     b = np.ascontiguousarray(bcflag, dtype=np.uint32)
+    sets, n = marker_sets(markers)
     _ck(lib().des_write_save(str(path).encode(), C.byref(mv), C.byref(params), abi.uptr(b), C.byref(v),
-                             C.byref(averages) if averages is not None else None), "des_write_save")
+                             C.byref(averages) if averages is not None else None, sets, n),
+        "des_write_save")
 
 
-def write_checkpoint(path, mesh, state, compensation_pressure):
-    """The .chkpt file of a frame (des_write_checkpoint)."""
+def write_checkpoint(path, mesh, state, compensation_pressure, markers=None):
+    """The .chkpt file of a frame (des_write_checkpoint), with its marker sets."""
     mv = mesh.view()
+    sets, n = marker_sets(markers)
     _ck(lib().des_write_checkpoint(str(path).encode(), C.byref(mv), state.time, compensation_pressure,
-                                   abi.dptr(state.volume_old)), "des_write_checkpoint")
+                                   abi.dptr(state.volume_old), sets, n), "des_write_checkpoint")
 
 
 def softf64_check(n, seed=20261203, device=0):

@@ -129,6 +129,12 @@ class StepReport(C.Structure):
                 ("closure_accepted", C.c_longlong), ("exact_returns", C.c_longlong)]
 
 
+class MarkerSet(C.Structure):
+    """des_marker_set: one marker set as the output files hold it."""
+    _fields_ = [("name", C.c_char_p), ("nmarkers", C.c_int), ("last_id", C.c_int),
+                ("eta", _dp), ("elem", _ip), ("mattype", _ip), ("id", _ip)]
+
+
 class SaveAverages(C.Structure):
     """des_save_averages: the averaging state of Output::average_fields."""
     _fields_ = [("coord0", _dp), ("strain0", _dp), ("stress_sum", _dp), ("dpls_sum", _dp),

@@ -375,13 +375,31 @@ typedef struct des_save_averages {
     int    interval;            /* mesh.quality_check_step_interval */
 } des_save_averages;
 
+/* One marker set (MarkerSet, markerset.hpp) as the output files hold it:
+ * its name ("markerset" for the material markers), the number of markers,
+ * the next id it would give out, and per marker the barycentric coordinates
+ * in its element, the element, the material type and the id. */
+typedef struct des_marker_set {
+    const char   *name;
+    int           nmarkers;
+    int           last_id;
+    const double *eta;          /* [nmarkers][4] */
+    const int    *elem;         /* [nmarkers] */
+    const int    *mattype;      /* [nmarkers] */
+    const int    *id;           /* [nmarkers] */
+} des_marker_set;
+
 /* Writes the .save file of one output frame to `path` as Output::_write
- * (output.cxx:73-198, BinaryOutput binaryio.cxx:44-131) does, byte for byte,
- * without marker sets: avg NULL for Output::write_exact or when averaging is
- * off.  Density, mesh quality, viscosity and material are computed on the
- * host with the reference's arithmetic.  Host-only; needs no GPU. */
+ * (output.cxx:73-198, BinaryOutput binaryio.cxx:44-131) does, byte for byte:
+ * avg NULL for Output::write_exact or when averaging is off; the nsets
+ * marker sets last (MarkerSet::write_save_file, markerset.cxx:452-483: size,
+ * marker coordinates from the nodes' coordinates, element, material, id) as
+ * with sim.has_marker_output on (nsets = 0 for off).  Density, mesh quality,
+ * viscosity, material and marker coordinates are computed on the host with
+ * the reference's arithmetic.  Host-only; needs no GPU. */
 int  des_write_save(const char *path, const des_mesh_view *mesh, const des_params *p,
-                    const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg);
+                    const unsigned *bcflag, const des_state_view *s, const des_save_averages *avg,
+                    const des_marker_set *sets, int nsets);
 
 /* Asynchronous output (the download of output.cxx's fields overlapped with
  * the next steps): des_gpu_output_snapshot copies the `mask` fields
@@ -397,9 +415,12 @@ int  des_gpu_output_fetch(des_gpu *g, des_state_view *host);
 int  des_gpu_output_wait(des_gpu *g, des_state_view *host);
 
 /* Writes the .chkpt file of a frame as Output::write_checkpoint
- * (output.cxx:270-296) does for a 3D model without marker sets.  Host-only. */
+ * (output.cxx:270-296) does for a 3D model, its nsets marker sets last
+ * (MarkerSet::write_chkpt_file, markerset.cxx:407-419: size and last id,
+ * barycentric coordinates, element, material, id).  Host-only. */
 int  des_write_checkpoint(const char *path, const des_mesh_view *mesh, double time,
-                          double compensation_pressure, const double *volume_old);
+                          double compensation_pressure, const double *volume_old,
+                          const des_marker_set *sets, int nsets);
 
 /* Output::average_fields on the device after every step from the next
  * des_gpu_step on (interval = mesh.quality_check_step_interval; 0 stops it). */

@@ -237,6 +237,8 @@ class RefOracle(_Base):
             L.dsr_output_begin.argtypes = [C.c_void_p, C.c_char_p, C.c_int, C.c_int, C.c_int]
             L.dsr_output_write.argtypes = [C.c_void_p, C.c_int]
             L.dsr_output_checkpoint.argtypes = [C.c_void_p]
+            L.dsr_add_markers.argtypes = [C.c_void_p, C.c_char_p, C.c_int, P(C.c_double), P(C.c_int),
+                                          P(C.c_int), C.c_int]
             L.dsr_elem_quality.argtypes = [C.c_void_p, P(C.c_double)]
             L.dsr_worst_elem_quality.argtypes = [C.c_void_p, P(C.c_int)]
             L.dsr_worst_elem_quality.restype = C.c_double
@@ -311,6 +313,15 @@ class RefOracle(_Base):
         a = np.zeros((n.value, 2), np.int32)
         self.L.dsr_bfacets(self.h, b, C.byref(n), abi.iptr(a))
         return a
+
+    def add_markers(self, name, eta, elem, mattype, marker_output=True):
+        """A marker set in var.markersets from the reference's own
+        MarkerSet::append_marker (ids 0..n-1); with marker_output the next
+        output_begin writes marker sets into .save files."""
+        self._mk = [np.ascontiguousarray(eta, np.float64).reshape(-1, 4),
+                    np.ascontiguousarray(elem, np.int32), np.ascontiguousarray(mattype, np.int32)]
+        self.L.dsr_add_markers(self.h, str(name).encode(), len(self._mk[1]), abi.dptr(self._mk[0]),
+                               abi.iptr(self._mk[1]), abi.iptr(self._mk[2]), int(marker_output))
 
     def output_begin(self, modelname, frame=0, averaged=False, interval=1):
         """The reference's Output for `modelname` (averaging in every later

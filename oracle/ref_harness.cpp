@@ -6,6 +6,7 @@
 // loop body of dynearthsol.cxx:358-394 without output and remeshing.
 // Used only to pin oracle/des_oracle.cpp and to write the golden fixtures.
 #include <cstring>
+#include <string>
 #include <limits>
 #include <new>
 #include <utility>
@@ -17,6 +18,7 @@
 #include "fields.hpp"
 #include "geometry.hpp"
 #include "ic.hpp"
+#include "markerset.hpp"
 #include "matprops.hpp"
 #include "mesh.hpp"
 #include "output.hpp"
@@ -29,6 +31,7 @@ struct dsr {
     Param param;
     Variables var;
     Output *out = nullptr;       // the reference's own output writer, when set up
+    bool marker_output = false;  // sim.has_marker_output of the next output_begin
 };
 
 namespace {
@@ -444,7 +447,7 @@ int dsr_output_begin(dsr *h, const char *modelname, int frame, int averaged, int
     delete h->out;
     h->param.sim.modelname = modelname;
     h->param.sim.is_outputting_averaged_fields = averaged != 0;
-    h->param.sim.has_marker_output = false;
+    h->param.sim.has_marker_output = h->marker_output;
     h->param.mesh.quality_check_step_interval = interval;
     h->out = new Output(h->param, 0.0, frame);
     return 0;
@@ -465,6 +468,19 @@ int dsr_output_write(dsr *h, int exact)
         h->out->write_exact(h->var);
     else
         h->out->write(h->var);
+    return 0;
+}
+
+// a marker set named `name` in var.markersets, built by the reference's own
+// MarkerSet::append_marker from the given markers (ids 0..n-1, last id n);
+// with marker_output the next output_begin turns sim.has_marker_output on
+int dsr_add_markers(dsr *h, const char *name, int n, const double *eta, const int *elem,
+                    const int *mattype, int marker_output)
+{
+    MarkerSet *ms = new MarkerSet(std::string(name));
+    for (int i = 0; i < n; ++i) ms->append_marker(eta + 4 * (size_t)i, elem[i], mattype[i]);
+    h->var.markersets.push_back(ms);
+    h->marker_output = marker_output != 0;
     return 0;
 }
 

@@ -83,3 +83,96 @@ def test_checkpoint_file_matches_the_reference(tmp_path):
     r.output_checkpoint(s)
     D.write_checkpoint(tmp_path / "ours.chkpt", c.mesh, s, r.compensation_pressure())
     assert (tmp_path / "ref.chkpt.000001").read_bytes() == (tmp_path / "ours.chkpt").read_bytes()
+
+
+def marker_sets(mesh, seed, sizes=(("markerset", 300), ("hydrous-markerset", 5000))):
+    """Marker sets with random barycentric positions in random elements; ids
+    0..n-1 and last id n, as MarkerSet::append_marker numbers them."""
+    rng = np.random.default_rng(seed)
+    sets = []
+    for name, n in sizes:
+        eta = rng.dirichlet(np.ones(4), size=n)
+        elem = rng.integers(0, mesh.nelem, n).astype(np.int32)
+        mattype = rng.integers(0, 3, n).astype(np.int32)
+        sets.append((name, eta, elem, mattype, np.arange(n, dtype=np.int32), n))
+    return sets
+
+
+def ref_with_markers(c, sets, marker_output):
+    r = RefOracle(c.mesh, c.params)
+    for name, eta, elem, mattype, _, _ in sets:
+        r.add_markers(name, eta, elem, mattype, marker_output)
+    return r
+
+
+@needs_ref
+def test_save_file_with_marker_sets_matches_the_reference(tmp_path):
+    """Two marker sets (the second one past MarkerSet's 4096 preallocated
+    markers) written into the .save file: marker coordinates summed from the
+    element's nodes as MarkerSet::write_save_file does."""
+    c = Case(W.CONFIGS["1"])
+    s = run(c, c.initial_state(), 15)
+    sets = marker_sets(c.mesh, 7)
+    r = ref_with_markers(c, sets, True)
+    r.output_begin(tmp_path / "ref", frame=3, averaged=False, interval=10)
+    r.output_write(s, exact=False)
+    D.write_save(tmp_path / "ours.save", c.mesh, c.params, c.oracle.bcflag(), s, markers=sets)
+    a = (tmp_path / "ref.save.000003").read_bytes()
+    b = (tmp_path / "ours.save").read_bytes()
+    assert a[:4096] == b[:4096]
+    assert a == b
+
+
+@needs_ref
+def test_checkpoint_file_with_marker_sets_matches_the_reference(tmp_path):
+    """The checkpoint always carries the marker sets (sizes with the last id,
+    barycentric coordinates, elements, material types, ids)."""
+    c = Case(W.CONFIGS["1"])
+    s = run(c, c.initial_state(), 6)
+    sets = marker_sets(c.mesh, 11)
+    r = ref_with_markers(c, sets, False)
+    r.output_begin(tmp_path / "ref", frame=1, averaged=False, interval=10)
+    r.output_checkpoint(s)
+    D.write_checkpoint(tmp_path / "ours.chkpt", c.mesh, s, r.compensation_pressure(), markers=sets)
+    a = (tmp_path / "ref.chkpt.000001").read_bytes()
+    b = (tmp_path / "ours.chkpt").read_bytes()
+    assert a[:4096] == b[:4096]
+    assert a == b
+
+
+def test_marker_set_layout_and_coordinates(tmp_path):
+    """Without the reference: the marker arrays follow bcflag under the set's
+    name, and each marker's coordinate is sum_k eta_k x(conn_k)."""
+    c = Case(W.CONFIGS["tiny"])
+    s = run(c, c.initial_state(), 2)
+    sets = marker_sets(c.mesh, 3, (("markerset", 40), ("empty-set", 0)))
+    D.write_save(tmp_path / "x.save", c.mesh, c.params, c.oracle.bcflag(), s, markers=sets)
+    raw = (tmp_path / "x.save").read_bytes()
+    head = raw[:4096].split(b"\0")[0].decode().splitlines()[1:]
+    names = [h.split("\t")[0] for h in head]
+    assert names[names.index("bcflag") + 1:] == [
+        "markerset size", "markerset.coord", "markerset.elem", "markerset.mattype", "markerset.id",
+        "empty-set size", "empty-set.coord", "empty-set.elem", "empty-set.mattype", "empty-set.id"]
+    pos = {h.split("\t")[0]: int(h.split("\t")[1]) for h in head}
+    _, eta, elem, mattype, ids, _ = sets[0]
+    assert np.frombuffer(raw[pos["markerset size"]:pos["markerset size"] + 4], np.int32)[0] == 40
+    xyz = np.frombuffer(raw[pos["markerset.coord"]:pos["markerset.elem"]], np.float64).reshape(-1, 3)
+    want = np.einsum("mk,mkj->mj", eta, s.coord[c.mesh.connectivity[elem]])
+    assert np.allclose(xyz, want, rtol=0, atol=1e-12 * np.abs(s.coord).max())
+    assert np.array_equal(np.frombuffer(raw[pos["markerset.elem"]:pos["markerset.mattype"]], np.int32), elem)
+    assert np.array_equal(np.frombuffer(raw[pos["markerset.mattype"]:pos["markerset.id"]], np.int32), mattype)
+    assert np.array_equal(np.frombuffer(raw[pos["markerset.id"]:pos["empty-set size"]], np.int32), ids)
+    assert pos["empty-set.id"] == len(raw)
+
+
+def test_marker_sets_out_of_range_are_refused(tmp_path):
+    c = Case(W.CONFIGS["tiny"])
+    s = c.initial_state()
+    name, eta, elem, mattype, ids, n = marker_sets(c.mesh, 5, (("markerset", 8),))[0]
+    bad = elem.copy()
+    bad[3] = c.mesh.nelem
+    with pytest.raises(Exception):
+        D.write_save(tmp_path / "x.save", c.mesh, c.params, c.oracle.bcflag(), s,
+                     markers=[(name, eta, bad, mattype, ids, n)])
+    with pytest.raises(Exception):
+        D.write_checkpoint(tmp_path / "x.chkpt", c.mesh, s, 0.0, markers=[(name, eta[:4], elem, mattype, ids, n)])
