@@ -64,7 +64,7 @@ class ClockSampler:
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -239,10 +239,43 @@ def train_closure(base, local, box=(60, 60, 12), nsteps=300, epochs=20):
     return net, info
 
 
+def profile_mlp_grad(args):
+    """The closure network's loss and gradient (k_mlp_grad) over a seeded
+    batch, `warmup` + `steps` calls, for ncu captures of the training kernel."""
+    import numpy as np
+    import des_gb300 as D
+    from des_gb300 import abi, closure
+    D.build()
+    rng = np.random.default_rng(3)
+    net = abi.Mlp()
+    for k in ("w1", "b1", "w2", "b2", "w3", "b3"):
+        a = net.arr(k)
+        a[...] = rng.normal(0, 0.3, a.shape)
+    net.arr("w1")[:, 14:] = 0
+    net.arr("w3")[7] = 0
+    net.arr("b3")[7] = 0
+    net.arr("in_scale")[:] = 1
+    net.arr("out_scale")[:] = 1
+    n = args.samples
+    x = np.zeros((n, 16), np.float32)
+    x[:, :14] = rng.normal(0, 1, (n, 14))
+    t = np.zeros((n, 8), np.float32)
+    t[:, :7] = rng.normal(0, 1, (n, 7))
+    for _ in range(args.warmup):
+        closure.loss_grad(net, x, t)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss, _ = closure.loss_grad(net, x, t)
+    print(json.dumps({"profile_form": "mlp_grad", "samples": n, "tiles": (n + 127) // 128, "loss": loss,
+                      "seconds_per_call_with_copies": (time.perf_counter() - t0) / args.steps}))
+
+
 def profile_form(args):
     """One form alone (for ncu captures): warm-up, then the timed steps."""
     import des_gb300 as D
     from des_gb300 import abi, workload as W
+    if args.profile_form == "mlp_grad":
+        return profile_mlp_grad(args)
     D.build()
     base = W.CONFIGS[args.config]
     cfg = base
@@ -803,8 +836,11 @@ def main():
                     help="skip configs 3, 4 and 5 at their stated sizes and step counts")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the 2,000-step FP32-against-FP64 accuracy run")
-    ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure"], default=None,
-                    help="run one form alone on --config/--box (for profiling)")
+    ap.add_argument("--profile-form", choices=["fp64", "fp32", "fp32_closure", "mlp_grad"], default=None,
+                    help="run one form alone on --config/--box (for profiling); mlp_grad: the "
+                    "closure network's loss and gradient over --samples seeded samples, --steps times")
+    ap.add_argument("--samples", type=int, default=152 * 8 * 128,
+                    help="samples of --profile-form mlp_grad")
     ap.add_argument("--box", default=None, help="NXxNYxNZ hexes instead of the config's box "
                     "(profiling of smaller cases)")
     args = ap.parse_args()

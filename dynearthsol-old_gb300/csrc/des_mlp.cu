@@ -1,9 +1,10 @@
 // Training and standalone evaluation of the learned return-map closure
 // (see des_mlp.cuh for the network).  Forward and backward passes run on the
 // fifth-generation tensor cores (des_mlp_tc.cuh: tcgen05 MMAs, BF16 operands
-// in shared memory, FP32 accumulators in tensor memory), one CTA per tile of
-// 128 samples; each tile's gradient is added to the global FP32 gradient with
-// atomics (one add per parameter per tile).  Adam keeps FP32 master weights
+// in shared memory, FP32 accumulators in tensor memory), persistent CTAs (at
+// most one per multiprocessor) over tiles of 128 samples; a CTA's weight
+// gradients accumulate in TMEM over its tiles and are added to the global
+// FP32 gradient with atomics once (one add per parameter per CTA).  Adam keeps FP32 master weights
 // and moments.
 #include <cuda_runtime.h>
 
@@ -42,22 +43,31 @@ __global__ void __launch_bounds__(kTcRows) k_mlp_forward(const float *P, const f
 {
     extern __shared__ unsigned char smem_raw[];
     MlpTcSmem &S = tc_smem(smem_raw);
-    const bool ok = mlptc_tile<false>(S, P, x, nullptr, n, (long long)blockIdx.x * kTile, 0.f, y, nullptr,
-                                      nullptr);
+    const bool ok = mlptc_tiles<false>(S, P, x, nullptr, n, 0, (n + kTile - 1) / kTile, 0.f, y, nullptr,
+                                       nullptr);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
 }
 
-// one tile: forward, loss, backward; grad += d(loss)/d(params) where loss is
-// the mean over `count` samples of the summed squared error of the 7 outputs
+// ntiles tiles from row_begin: forward, loss, backward; grad +=
+// d(loss)/d(params) where loss is the mean over `count` samples of the
+// summed squared error of the 7 outputs
 __global__ void __launch_bounds__(kTcRows) k_mlp_grad(const float *P, const float *x, const float *yt,
-                                                      long long n, long long row_begin, float inv_count,
-                                                      float *grad, double *loss, int *err)
+                                                      long long n, long long row_begin, long long ntiles,
+                                                      float inv_count, float *grad, double *loss, int *err)
 {
     extern __shared__ unsigned char smem_raw[];
     MlpTcSmem &S = tc_smem(smem_raw);
-    const bool ok = mlptc_tile<true>(S, P, x, yt, n, row_begin + (long long)blockIdx.x * kTile, inv_count,
-                                     nullptr, grad, loss);
+    const bool ok = mlptc_tiles<true>(S, P, x, yt, n, row_begin, ntiles, inv_count, nullptr, grad, loss);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+}
+
+// CTAs for ntiles tiles: one per multiprocessor at most (persistent)
+int tile_grid(long long ntiles)
+{
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (int)std::max<long long>(1, std::min<long long>(ntiles, sms > 0 ? sms : 1));
 }
 
 // Adam (Kingma & Ba 2015) on the flat FP32 parameters; padded entries stay 0
@@ -140,7 +150,7 @@ int des_mlp_forward(const des_mlp *net, const float *x, long long n, float *y)
         cudaMemcpy(dx.p, x, sizeof(float) * n * kMlpIn, cudaMemcpyHostToDevice) ||
         cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
-    int grid = (int)((n + kTile - 1) / kTile);
+    const int grid = tile_grid((n + kTile - 1) / kTile);
     k_mlp_forward<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), n, dy.as<float>(),
                                                       de.as<int>());
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return DES_ERR_CUDA;
@@ -167,9 +177,9 @@ int des_mlp_loss_grad(const des_mlp *net, const float *x, const float *y, long l
         cudaMemset(dg.p, 0, sizeof(float) * kNParams) || cudaMemset(dl.p, 0, sizeof(double)) ||
         cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
-    int grid = (int)((n + kTile - 1) / kTile);
-    k_mlp_grad<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n, 0,
-                                                   1.f / (float)n, dg.as<float>(), dl.as<double>(), de.as<int>());
+    const long long ntiles = (n + kTile - 1) / kTile;
+    k_mlp_grad<<<tile_grid(ntiles), kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(),
+                                                                n, 0, ntiles, 1.f / (float)n, dg.as<float>(), dl.as<double>(), de.as<int>());
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return DES_ERR_CUDA;
     if (int rc = read_err(de.as<int>())) return rc;
     std::vector<float> G(kNParams);
@@ -212,14 +222,14 @@ int des_mlp_train(des_mlp *net, const float *x, const float *y, long long n, int
         cudaMemset(dl.p, 0, sizeof(double) * (size_t)steps) || cudaMemset(de.p, 0, sizeof(int)))
         return DES_ERR_CUDA;
     const long long nb = n / batch;
-    const int grid = batch / kTile;
+    const int ntiles = batch / kTile, grid = tile_grid(ntiles);
     for (int s = 0; s < steps; ++s) {
         long long begin = (long long)(s % nb) * batch;
         // cosine decay of the step size from lr to lr / 100
         const float lr_s = lr * (0.01f + 0.99f * 0.5f * (1.f + cosf(3.14159265f * (float)s / (float)steps)));
         cudaMemsetAsync(dg.p, 0, sizeof(float) * kNParams);
         k_mlp_grad<<<grid, kTcRows, kMlpTcSmemBytes>>>(dP.as<float>(), dx.as<float>(), dy.as<float>(), n,
-                                                       begin, 1.f / (float)batch, dg.as<float>(),
+                                                       begin, ntiles, 1.f / (float)batch, dg.as<float>(),
                                                        dl.as<double>() + s, de.as<int>());
         k_adam<<<(kNParams + 255) / 256, 256>>>(dP.as<float>(), dm.as<float>(), dv.as<float>(),
                                                dg.as<float>(), s + 1, lr_s);

@@ -1,6 +1,6 @@
 // The learned closure's network (14 -> 64 -> 64 -> 7, des_mlp.cuh) on the
-// fifth-generation tensor cores: one CTA of 128 threads per tile of 128
-// samples, BF16 operands in shared memory (K-major, no swizzle, des_tc.cuh),
+// fifth-generation tensor cores: CTAs of 128 threads over tiles of 128
+// samples (persistent: a CTA takes every gridDim.x-th tile), BF16 operands in shared memory (K-major, no swizzle, des_tc.cuh),
 // FP32 accumulators in tensor memory, every MMA issued by one thread and
 // committed to an mbarrier; the other threads move data between TMEM and
 // shared memory (tcgen05.ld, one sample per thread: TMEM lane = sample).
@@ -84,12 +84,13 @@ __device__ __forceinline__ uint64_t desc(const unsigned char *tile, int K, int k
     return tc::smem_desc(tc::smem_addr(tile) + 256u * (uint32_t)kk, 128u, (uint32_t)(16 * K));
 }
 
-// D[tmem col] = A B^T over K (K / 16 MMAs), then (with commit_now) a commit
+// D[tmem col] = A B^T over K (K / 16 MMAs), or D += A B^T with accumulate,
+// then (with commit_now) a commit
 __device__ __forceinline__ void gemm(uint32_t d, const unsigned char *A, const unsigned char *B, int K, int N,
-                                     uint64_t *bar, bool commit_now)
+                                     uint64_t *bar, bool commit_now, bool accumulate = false)
 {
     const uint32_t id = tc::idesc_bf16(kTcRows, N);
-    for (int kk = 0; kk < K / 16; ++kk) tc::mma_bf16(d, desc(A, K, kk), desc(B, K, kk), id, kk > 0);
+    for (int kk = 0; kk < K / 16; ++kk) tc::mma_bf16(d, desc(A, K, kk), desc(B, K, kk), id, accumulate || kk > 0);
     if (commit_now) tc::commit(bar);
 }
 
@@ -150,14 +151,18 @@ __device__ __forceinline__ void mlptc_load(MlpTcSmem &S, const float *P, bool ba
         }
 }
 
-// One tile of 128 samples from row0 (128 threads): the forward pass, writing
-// y_out [n][8]; with BACKWARD instead the loss (added to *loss) and the
-// gradient (added to grad, the flat FP32 layout of P, with atomics).
-// Returns false after a tensor-core wait timed out; TMEM is released either
-// way.
+// Tiles k = blockIdx.x, blockIdx.x + gridDim.x, ... (< ntiles) of 128
+// samples from row_begin, by one CTA of 128 threads: the forward pass,
+// writing y_out [n][8]; with BACKWARD instead the loss (added to *loss) and
+// the gradient (added to grad, the flat FP32 layout of P).  The weights are
+// staged once per CTA; the weight and bias gradients accumulate in TMEM over
+// the CTA's tiles and are added to grad with one atomic per parameter per
+// CTA at the end.  Returns false after a tensor-core wait timed out; TMEM is
+// released either way.
 template <bool BACKWARD>
-__device__ bool mlptc_tile(MlpTcSmem &S, const float *P, const float *x, const float *yt, long long n,
-                           long long row0, float inv_count, float *y_out, float *grad, double *loss)
+__device__ bool mlptc_tiles(MlpTcSmem &S, const float *P, const float *x, const float *yt, long long n,
+                            long long row_begin, long long ntiles, float inv_count, float *y_out, float *grad,
+                            double *loss)
 {
     using namespace mlptc;
     const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -165,138 +170,155 @@ __device__ bool mlptc_tile(MlpTcSmem &S, const float *P, const float *x, const f
     if (w == 0) tc::tmem_alloc(&S.tmem, kTcCols);
     if (t == 0) tc::mbar_init(&S.bar, 1);
     mlptc_load(S, P, BACKWARD);
-    const long long row = row0 + t;
-    const bool valid = row < n;
-    {
-        float v[16];
-        for (int k = 0; k < 16; ++k) v[k] = valid ? x[row * kMlpIn + k] : 0.f;
-        put8(S.x, t, 0, 16, v);
-        put8(S.x, t, 8, 16, v + 8);
-        if (BACKWARD)
-            for (int k = 0; k < 16; ++k) put_bf16(S.bg, 64 + k, t, kTcRows, v[k]);
-    }
-    hand_to_tensor_cores();
     const uint32_t tm = S.tmem;
     int phase = 0;
-    bool ok = true;
-
-    // H1 = relu(X W1^T + b1)
-    if (t == 0) gemm(tm + 0, S.x, S.w1, 16, 64, &S.bar, true);
-    ok = wait_commit(&S.bar, phase++);
-    if (ok)
-        for (int c = 0; c < 64; c += 16) {
+    bool ok = true, first = true;
+    // this thread's sample of a tile: inputs and (BACKWARD) targets, loaded one
+    // tile ahead so that the loads run under the previous tile's MMAs
+    float xn[16], yn[kMlpOut] = {};
+    auto fetch = [&](long long tile) {
+        const long long r = row_begin + tile * kTcRows + t;
+        const bool v = tile < ntiles && r < n;
+        for (int k = 0; k < 16; ++k) xn[k] = v ? x[r * kMlpIn + k] : 0.f;
+        if (BACKWARD)
+            for (int j = 0; j < kMlpOut; ++j) yn[j] = v ? yt[r * kMlpOut + j] : 0.f;
+    };
+    fetch(blockIdx.x);
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, first = false) {
+        const long long row = row_begin + tile * kTcRows + t;
+        const bool valid = row < n;
+        float ycur[kMlpOut];
+        {
             float v[16];
-            tc::tmem_ld16(tm + lane_base + c, v);
-            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + S.b1[c + i], 0.f);
-            put8(S.h1, t, c, 64, v);
-            put8(S.h1, t, c + 8, 64, v + 8);
+            for (int k = 0; k < 16; ++k) v[k] = xn[k];
+            for (int j = 0; j < kMlpOut; ++j) ycur[j] = yn[j];
+            put8(S.x, t, 0, 16, v);
+            put8(S.x, t, 8, 16, v + 8);
             if (BACKWARD)
-                for (int i = 0; i < 16; ++i) put_bf16(S.bg, c + i, t, kTcRows, v[i]);
+                for (int k = 0; k < 16; ++k) put_bf16(S.bg, 64 + k, t, kTcRows, v[k]);
         }
-    hand_to_tensor_cores();
-    // H2 = relu(H1 W2^T + b2)
-    if (ok) {
-        if (t == 0) gemm(tm + 64, S.h1, S.w2, 64, 64, &S.bar, true);
-        ok = wait_commit(&S.bar, phase++);
-    }
-    if (ok)
-        for (int c = 0; c < 64; c += 16) {
-            float v[16];
-            tc::tmem_ld16(tm + lane_base + 64 + c, v);
-            for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + S.b2[c + i], 0.f);
-            put8(S.h2, t, c, 64, v);
-            put8(S.h2, t, c + 8, 64, v + 8);
-            if (BACKWARD)
-                for (int i = 0; i < 16; ++i) put_bf16(S.h2t, c + i, t, kTcRows, v[i]);
-        }
-    hand_to_tensor_cores();
-    // Y = H2 W3^T + b3
-    if (ok) {
-        if (t == 0) gemm(tm + 128, S.h2, S.w3, 64, 16, &S.bar, true);
-        ok = wait_commit(&S.bar, phase++);
-    }
-    if (ok) {
-        float v[16];
-        tc::tmem_ld16(tm + lane_base + 128, v);
-        for (int j = 0; j < 16; ++j) v[j] = j < kMlpOutUsed ? v[j] + S.b3[j] : 0.f;
-        if (!BACKWARD) {
-            if (valid)
-                for (int j = 0; j < kMlpOut; ++j) y_out[row * kMlpOut + j] = v[j];
-        } else {
-            double l = 0.0;
-            float g[16];
-            for (int j = 0; j < 16; ++j) {
-                const float e = (valid && j < kMlpOutUsed) ? v[j] - yt[row * kMlpOut + j] : 0.f;
-                l += (double)e * e;
-                g[j] = 2.f * e * inv_count;
-            }
-            put8(S.dy, t, 0, 16, g);
-            for (int j = 0; j < kMlpOutUsed; ++j) put_bf16(S.dyt, j, t, kTcRows, g[j]);
-            for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
-            if (lane == 0) atomicAdd(loss, l * inv_count);
-        }
-    }
-    if (BACKWARD) {
+        fetch(tile + gridDim.x);
         hand_to_tensor_cores();
-        // dH2 (before the mask) and dW3^T, db3
-        if (ok) {
-            if (t == 0) {
-                gemm(tm + 0, S.dy, S.w3t, 16, 64, &S.bar, false);
-                gemm(tm + 240, S.h2t, S.dyt, kTcRows, 16, &S.bar, true);
-            }
-            ok = wait_commit(&S.bar, phase++);
-        }
+
+        // H1 = relu(X W1^T + b1)
+        if (t == 0) gemm(tm + 0, S.x, S.w1, 16, 64, &S.bar, true);
+        ok = wait_commit(&S.bar, phase++);
         if (ok)
             for (int c = 0; c < 64; c += 16) {
                 float v[16];
                 tc::tmem_ld16(tm + lane_base + c, v);
-                for (int i = 0; i < 16; ++i) v[i] = get_bf16(S.h2, t, c + i, 64) > 0.f ? v[i] : 0.f;
-                put8(S.dh2, t, c, 64, v);
-                put8(S.dh2, t, c + 8, 64, v + 8);
-                for (int i = 0; i < 16; ++i) put_bf16(S.ag, c + i, t, kTcRows, v[i]);
+                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + S.b1[c + i], 0.f);
+                put8(S.h1, t, c, 64, v);
+                put8(S.h1, t, c + 8, 64, v + 8);
+                if (BACKWARD)
+                    for (int i = 0; i < 16; ++i) put_bf16(S.bg, c + i, t, kTcRows, v[i]);
             }
         hand_to_tensor_cores();
-        // dH1 (before the mask)
+        // H2 = relu(H1 W2^T + b2)
         if (ok) {
-            if (t == 0) gemm(tm + 64, S.dh2, S.w2t, 64, 64, &S.bar, true);
+            if (t == 0) gemm(tm + 64, S.h1, S.w2, 64, 64, &S.bar, true);
             ok = wait_commit(&S.bar, phase++);
         }
         if (ok)
             for (int c = 0; c < 64; c += 16) {
                 float v[16];
                 tc::tmem_ld16(tm + lane_base + 64 + c, v);
-                for (int i = 0; i < 16; ++i) {
-                    const float h = get_bf16(S.h1, t, c + i, 64);
-                    put_bf16(S.ag, 64 + c + i, t, kTcRows, h > 0.f ? v[i] : 0.f);
-                }
+                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i] + S.b2[c + i], 0.f);
+                put8(S.h2, t, c, 64, v);
+                put8(S.h2, t, c + 8, 64, v + 8);
+                if (BACKWARD)
+                    for (int i = 0; i < 16; ++i) put_bf16(S.h2t, c + i, t, kTcRows, v[i]);
             }
         hand_to_tensor_cores();
-        // [dW2 | . | db2] over lanes 0-63, [. | dW1 | db1] over lanes 64-127
+        // Y = H2 W3^T + b3
         if (ok) {
-            if (t == 0) gemm(tm + 144, S.ag, S.bg, kTcRows, 96, &S.bar, true);
+            if (t == 0) gemm(tm + 128, S.h2, S.w3, 64, 16, &S.bar, true);
             ok = wait_commit(&S.bar, phase++);
         }
         if (ok) {
-            const int m = t;                   // this thread's TMEM lane
             float v[16];
-            if (w < 2) {
-                for (int c = 0; c < 64; c += 16) {
-                    tc::tmem_ld16(tm + lane_base + 144 + c, v);
-                    for (int i = 0; i < 16; ++i) atomicAdd(grad + oW2 + m * 64 + c + i, v[i]);
-                }
-                tc::tmem_ld16(tm + lane_base + 144 + 80, v);
-                atomicAdd(grad + oB2 + m, v[0]);
-                tc::tmem_ld16(tm + lane_base + 240, v);            // row m of dW3^T
-                for (int j = 0; j < kMlpOutUsed; ++j) atomicAdd(grad + oW3 + j * 64 + m, v[j]);
+            tc::tmem_ld16(tm + lane_base + 128, v);
+            for (int j = 0; j < 16; ++j) v[j] = j < kMlpOutUsed ? v[j] + S.b3[j] : 0.f;
+            if (!BACKWARD) {
+                if (valid)
+                    for (int j = 0; j < kMlpOut; ++j) y_out[row * kMlpOut + j] = v[j];
             } else {
-                tc::tmem_ld16(tm + lane_base + 144 + 64, v);
-                for (int i = 0; i < 16; ++i) atomicAdd(grad + oW1 + (m - 64) * 16 + i, v[i]);
-                tc::tmem_ld16(tm + lane_base + 144 + 80, v);
-                atomicAdd(grad + oB1 + (m - 64), v[0]);
-                tc::tmem_ld16(tm + lane_base + 240, v);            // lane 64: db3
-                if (m == 64)
-                    for (int j = 0; j < kMlpOutUsed; ++j) atomicAdd(grad + oB3 + j, v[j]);
+                double l = 0.0;
+                float g[16];
+                for (int j = 0; j < 16; ++j) {
+                    const float e = (valid && j < kMlpOutUsed) ? v[j] - ycur[j] : 0.f;
+                    l += (double)e * e;
+                    g[j] = 2.f * e * inv_count;
+                }
+                put8(S.dy, t, 0, 16, g);
+                for (int j = 0; j < kMlpOutUsed; ++j) put_bf16(S.dyt, j, t, kTcRows, g[j]);
+                for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+                if (lane == 0) atomicAdd(loss, l * inv_count);
             }
+        }
+        if (BACKWARD) {
+            hand_to_tensor_cores();
+            // dH2 (before the mask) and dW3^T, db3 (accumulated over the tiles)
+            if (ok) {
+                if (t == 0) {
+                    gemm(tm + 0, S.dy, S.w3t, 16, 64, &S.bar, false);
+                    gemm(tm + 240, S.h2t, S.dyt, kTcRows, 16, &S.bar, true, !first);
+                }
+                ok = wait_commit(&S.bar, phase++);
+            }
+            if (ok)
+                for (int c = 0; c < 64; c += 16) {
+                    float v[16];
+                    tc::tmem_ld16(tm + lane_base + c, v);
+                    for (int i = 0; i < 16; ++i) v[i] = get_bf16(S.h2, t, c + i, 64) > 0.f ? v[i] : 0.f;
+                    put8(S.dh2, t, c, 64, v);
+                    put8(S.dh2, t, c + 8, 64, v + 8);
+                    for (int i = 0; i < 16; ++i) put_bf16(S.ag, c + i, t, kTcRows, v[i]);
+                }
+            hand_to_tensor_cores();
+            // dH1 (before the mask)
+            if (ok) {
+                if (t == 0) gemm(tm + 64, S.dh2, S.w2t, 64, 64, &S.bar, true);
+                ok = wait_commit(&S.bar, phase++);
+            }
+            if (ok)
+                for (int c = 0; c < 64; c += 16) {
+                    float v[16];
+                    tc::tmem_ld16(tm + lane_base + 64 + c, v);
+                    for (int i = 0; i < 16; ++i) {
+                        const float h = get_bf16(S.h1, t, c + i, 64);
+                        put_bf16(S.ag, 64 + c + i, t, kTcRows, h > 0.f ? v[i] : 0.f);
+                    }
+                }
+            hand_to_tensor_cores();
+            // [dW2 | . | db2] over lanes 0-63, [. | dW1 | db1] over lanes 64-127
+            // (accumulated over the tiles)
+            if (ok) {
+                if (t == 0) gemm(tm + 144, S.ag, S.bg, kTcRows, 96, &S.bar, true, !first);
+                ok = wait_commit(&S.bar, phase++);
+            }
+        }
+    }
+    if (BACKWARD && ok && !first) {
+        const int m = t;                       // this thread's TMEM lane
+        float v[16];
+        if (w < 2) {
+            for (int c = 0; c < 64; c += 16) {
+                tc::tmem_ld16(tm + lane_base + 144 + c, v);
+                for (int i = 0; i < 16; ++i) atomicAdd(grad + oW2 + m * 64 + c + i, v[i]);
+            }
+            tc::tmem_ld16(tm + lane_base + 144 + 80, v);
+            atomicAdd(grad + oB2 + m, v[0]);
+            tc::tmem_ld16(tm + lane_base + 240, v);            // row m of dW3^T
+            for (int j = 0; j < kMlpOutUsed; ++j) atomicAdd(grad + oW3 + j * 64 + m, v[j]);
+        } else {
+            tc::tmem_ld16(tm + lane_base + 144 + 64, v);
+            for (int i = 0; i < 16; ++i) atomicAdd(grad + oW1 + (m - 64) * 16 + i, v[i]);
+            tc::tmem_ld16(tm + lane_base + 144 + 80, v);
+            atomicAdd(grad + oB1 + (m - 64), v[0]);
+            tc::tmem_ld16(tm + lane_base + 240, v);            // lane 64: db3
+            if (m == 64)
+                for (int j = 0; j < kMlpOutUsed; ++j) atomicAdd(grad + oB3 + j, v[j]);
         }
     }
     tc::fence_before_sync();

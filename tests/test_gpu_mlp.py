@@ -34,7 +34,9 @@ def _data(seed, n):
     return x, y
 
 
-@pytest.mark.parametrize("n", [1, 17, 64, 1000])
+# 38,989 samples: 305 tiles, the last one ragged, so that the persistent CTAs
+# (one per multiprocessor) take several tiles each
+@pytest.mark.parametrize("n", [1, 17, 64, 1000, 38989])
 def test_forward_matches_cpu(gpu, n):
     net = _net(1)
     x, _ = _data(2, n)
@@ -45,7 +47,7 @@ def test_forward_matches_cpu(gpu, n):
     assert np.all(y[:, 7] == 0)
 
 
-@pytest.mark.parametrize("n", [64, 200, 4096])
+@pytest.mark.parametrize("n", [64, 200, 4096, 38989])
 def test_gradients_match_cpu(gpu, n):
     net = _net(3)
     x, t = _data(4, n)
