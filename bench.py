@@ -40,7 +40,7 @@ B_NODE = 3 * 8 * 2 * 2 + 8 * 2 + 4
 
 # DRAM bytes (read + written) per element of each FP64 pass from one ncu
 # capture of the pass alone on a 100x100x40 box of config 2's physics
-TRAFFIC_PER_ELEM = {"N-A": 95.0, "E-B": 347.6, "N-B": 26.3, "E-C": 292.4, "N-C": 136.7, "E-A": 562.5}
+TRAFFIC_PER_ELEM = {"N-A": 95.0, "E-B": 357.1, "N-B": 26.3, "E-C": 310.6, "N-C": 136.7, "E-A": 562.5}
 
 
 def peaks():
