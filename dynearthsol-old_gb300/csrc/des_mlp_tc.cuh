@@ -321,6 +321,9 @@ __device__ bool mlptc_tiles(MlpTcSmem &S, const float *P, const float *x, const 
                 for (int j = 0; j < kMlpOutUsed; ++j) atomicAdd(grad + oB3 + j, v[j]);
         }
     }
+    // after a time-out, give the MMAs of that phase one more bounded wait
+    // before their TMEM is released
+    if (!ok) tc::mbar_wait(&S.bar, (uint32_t)((phase - 1) & 1));
     tc::fence_before_sync();
     __syncthreads();
     if (w == 0) tc::tmem_dealloc(tm, kTcCols);
