@@ -622,8 +622,9 @@ __device__ __forceinline__ double tet_volume(const double *d0, const double *d1,
                     x23 * (y12 * z01 - y01 * z12));
 }
 
-// geometry.cxx:53-83 (3D)
-__device__ __forceinline__ double tri_area(const double *a, const double *b, const double *c)
+// geometry.cxx:53-83 (3D): the squared norm of the facet's cross product,
+// whose sqrt / 2 is the facet's area
+__device__ __forceinline__ double tri_area2(const double *a, const double *b, const double *c)
 {
     double ab0 = b[0] - a[0], ab1 = b[1] - a[1];
     double ac0 = c[0] - a[0], ac1 = c[1] - a[1];
@@ -631,7 +632,13 @@ __device__ __forceinline__ double tri_area(const double *a, const double *b, con
     double d0 = ab1 * ac2 - ab2 * ac1;
     double d1 = ab2 * ac0 - ab0 * ac2;
     double d2 = ab0 * ac1 - ab1 * ac0;
-    return sqrt(d0 * d0 + d1 * d1 + d2 * d2) / 2;
+    return d0 * d0 + d1 * d1 + d2 * d2;
+}
+
+// geometry.cxx:53-83 (3D)
+__device__ __forceinline__ double tri_area(const double *a, const double *b, const double *c)
+{
+    return sqrt(tri_area2(a, b, c)) / 2;
 }
 
 // geometry.cxx:472-509 (3D): 216 sqrt(3) V^2 / (sum of the face areas)^3, 1
@@ -803,11 +810,16 @@ __device__ __forceinline__ void conduction(const double *dx, const double *dy, c
     }
 }
 
-// geometry.cxx:280-293 for one element: 3 V / (largest facet area)
+// geometry.cxx:280-293 for one element: 3 V / (largest facet area).  The
+// largest area is taken among the squared norms and rooted once: a correctly
+// rounded sqrt and the exact halving keep the order (equal roots of unequal
+// squares are equal values) and NaN stays NaN, so smax selects the same
+// value as among the four areas.
 __device__ __forceinline__ double min_height(const double X[4][3], double vol)
 {
-    double maxa = smax(smax(tri_area(X[0], X[1], X[2]), tri_area(X[0], X[1], X[3])),
-                       smax(tri_area(X[2], X[3], X[0]), tri_area(X[2], X[3], X[1])));
+    double m2 = smax(smax(tri_area2(X[0], X[1], X[2]), tri_area2(X[0], X[1], X[3])),
+                     smax(tri_area2(X[2], X[3], X[0]), tri_area2(X[2], X[3], X[1])));
+    double maxa = sqrt(m2) / 2;
     return 3 * vol / maxa;
 }
 
