@@ -650,9 +650,13 @@ __device__ __forceinline__ double elem_quality(const double X[4][3], double vol,
     return nf * vol * vol / (area_sum * area_sum * area_sum);
 }
 
-// geometry.cxx:410-452; X[v][d] are the four vertex coordinates
+// geometry.cxx:410-452; X[v][d] are the four vertex coordinates.  r1 and
+// r3 receive the bracketed cross products of nodes 1 and 3 (before the
+// scaling by iv); they are, bit for bit, the cross products tri_area forms
+// for the facets (2, 3, 0) and (0, 1, 2): each edge difference here is the
+// other's or its exact negative, and the products commute.
 __device__ __forceinline__ void shape_fn(const double X[4][3], double vol, double dx[4], double dy[4],
-                                         double dz[4])
+                                         double dz[4], double r1[3], double r3[3])
 {
     const double *d0 = X[0], *d1 = X[1], *d2 = X[2], *d3 = X[3];
     double iv = 1 / (6 * vol);
@@ -662,18 +666,31 @@ __device__ __forceinline__ void shape_fn(const double X[4][3], double vol, doubl
     double y12 = d1[1] - d2[1], y13 = d1[1] - d3[1], y23 = d2[1] - d3[1];
     double z01 = d0[2] - d1[2], z02 = d0[2] - d2[2], z03 = d0[2] - d3[2];
     double z12 = d1[2] - d2[2], z13 = d1[2] - d3[2], z23 = d2[2] - d3[2];
+    r1[0] = y02 * z23 - y23 * z02;
+    r1[1] = z02 * x23 - z23 * x02;
+    r1[2] = x02 * y23 - x23 * y02;
+    r3[0] = y01 * z02 - y02 * z01;
+    r3[1] = z01 * x02 - z02 * x01;
+    r3[2] = x01 * y02 - x02 * y01;
     dx[0] = iv * (y13 * z12 - y12 * z13);
-    dx[1] = iv * (y02 * z23 - y23 * z02);
+    dx[1] = iv * r1[0];
     dx[2] = iv * (y13 * z03 - y03 * z13);
-    dx[3] = iv * (y01 * z02 - y02 * z01);
+    dx[3] = iv * r3[0];
     dy[0] = iv * (z13 * x12 - z12 * x13);
-    dy[1] = iv * (z02 * x23 - z23 * x02);
+    dy[1] = iv * r1[1];
     dy[2] = iv * (z13 * x03 - z03 * x13);
-    dy[3] = iv * (z01 * x02 - z02 * x01);
+    dy[3] = iv * r3[1];
     dz[0] = iv * (x13 * y12 - x12 * y13);
-    dz[1] = iv * (x02 * y23 - x23 * y02);
+    dz[1] = iv * r1[2];
     dz[2] = iv * (x13 * y03 - x03 * y13);
-    dz[3] = iv * (x01 * y02 - x02 * y01);
+    dz[3] = iv * r3[2];
+}
+
+__device__ __forceinline__ void shape_fn(const double X[4][3], double vol, double dx[4], double dy[4],
+                                         double dz[4])
+{
+    double r1[3], r3[3];
+    shape_fn(X, vol, dx, dy, dz, r1, r3);
 }
 
 // fields.cxx:193-241: D = sym(grad v) from the four nodal velocities V[i][d]
@@ -819,6 +836,17 @@ __device__ __forceinline__ double min_height(const double X[4][3], double vol)
 {
     double m2 = smax(smax(tri_area2(X[0], X[1], X[2]), tri_area2(X[0], X[1], X[3])),
                      smax(tri_area2(X[2], X[3], X[0]), tri_area2(X[2], X[3], X[1])));
+    double maxa = sqrt(m2) / 2;
+    return 3 * vol / maxa;
+}
+
+// the same with the cross products of the facets (0, 1, 2) and (2, 3, 0)
+// taken from shape_fn (r3 and r1)
+__device__ __forceinline__ double min_height(const double X[4][3], double vol, const double r1[3],
+                                             const double r3[3])
+{
+    double m2 = smax(smax(r3[0] * r3[0] + r3[1] * r3[1] + r3[2] * r3[2], tri_area2(X[0], X[1], X[3])),
+                     smax(r1[0] * r1[0] + r1[1] * r1[1] + r1[2] * r1[2], tri_area2(X[2], X[3], X[1])));
     double maxa = sqrt(m2) / 2;
     return 3 * vol / maxa;
 }

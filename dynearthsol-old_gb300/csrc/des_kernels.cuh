@@ -1214,13 +1214,13 @@ __global__ void __launch_bounds__(128, 6) k_fe_a(Dev d, int e0, unsigned nblocks
         d.vol_old[e] = d.vol[e];
         d.vol[e] = vol;
         if (not_positive(vol)) atomicOr(&d.clk->status, 0x4u);
-        double dx[4], dy[4], dz[4];
-        shape_fn(X, vol, dx, dy, dz);
+        double dx[4], dy[4], dz[4], r1[3], r3[3];
+        shape_fn(X, vol, dx, dy, dz, r1, r3);
         store_shp(d, e, dx, dy, dz);
         // the element's dt candidates here, so that the coordinates are dead
         // before the rotation's registers are needed (geometry.cxx:280-300)
         if (dt_step) {
-            minh = min_height(X, vol);
+            minh = min_height(X, vol, r1, r3);
             dtd = 0.5 * minh * minh / K.therm_diff_max;
         }
         const Mix &x = K.M.mix[d.mix[e]];
