@@ -1018,7 +1018,6 @@ int des_gpu_create(const des_mesh_view *m, const des_params *p, int device, des_
     Clock c0;
     std::memset(&c0, 0, sizeof(c0));
     c0.minl = ~0ULL;
-    c0.dtdiff = ~0ULL;
     if (cudaMemcpy(g->dclk, &c0, sizeof(Clock), cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(DES_ERR_CUDA);
     if ((rc = build_consts(g))) return fail(rc);

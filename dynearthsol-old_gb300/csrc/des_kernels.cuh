@@ -72,7 +72,7 @@ struct Consts {
 struct Clock {
     double dt, time;
     int steps, mass_valid;
-    unsigned long long minl, dtdiff;   // order_bits of running minima
+    unsigned long long minl;           // order_bits of the running minimum height
     unsigned blocks_done, status;
     unsigned long long ql, eig;
     unsigned long long nlog;                    // return-map records seen (logging launches)
@@ -426,38 +426,33 @@ __device__ __forceinline__ void vbc_node(const Consts &K, unsigned flag, R v[3])
     }
 }
 
-// block-level minimum of two values + the last block turns the global minima
-// into dt (geometry.cxx:311-325).  No thread waits on another block.
-// nblocks: the blocks of every launch that contributes (E-A may run as
-// several launches over consecutive element ranges); the last to finish
-// forms dt
-__device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff, bool active,
-                                       unsigned nblocks)
+// block-level minimum of the elements' heights + the last block turns the
+// global minimum into dt (geometry.cxx:311-325).  No thread waits on another
+// block.  nblocks: the blocks of every launch that contributes (E-A may run
+// as several launches over consecutive element ranges); the last to finish
+// forms dt.  The reference's dt_diffusion, the minimum over the elements of
+// 0.5 h h / therm_diff_max (geometry.cxx:305-307), is that expression of the
+// minimum height: for h >= 0 it is non-decreasing in h under round to
+// nearest (0.5 h exact, then a product and a quotient by a positive
+// constant, each rounded monotonically), so the minimum commutes with it;
+// where a height is negative, dt_advection <= 0 is the smaller term either
+// way.
+__device__ void dt_reduce_and_finalize(const Dev &d, double minh, bool active, unsigned nblocks)
 {
-    __shared__ unsigned long long s_min[32], s_dif[32];
+    __shared__ unsigned long long s_min[32];
     __shared__ bool s_last;
     unsigned long long a = active ? order_bits(minh) : ~0ULL;
-    unsigned long long b = active ? order_bits(dtdiff) : ~0ULL;
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long a2 = __shfl_down_sync(0xffffffffu, a, o);
-        unsigned long long b2 = __shfl_down_sync(0xffffffffu, b, o);
         a = a2 < a ? a2 : a;
-        b = b2 < b ? b2 : b;
     }
     int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) {
-        s_min[warp] = a;
-        s_dif[warp] = b;
-    }
+    if (lane == 0) s_min[warp] = a;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long ma = ~0ULL, mb = ~0ULL;
-        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) {
-            ma = s_min[w] < ma ? s_min[w] : ma;
-            mb = s_dif[w] < mb ? s_dif[w] : mb;
-        }
+        unsigned long long ma = ~0ULL;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) ma = s_min[w] < ma ? s_min[w] : ma;
         if (ma != ~0ULL) atomicMin(&d.clk->minl, ma);
-        if (mb != ~0ULL) atomicMin(&d.clk->dtdiff, mb);
         __threadfence();
         unsigned done = atomicAdd(&d.clk->blocks_done, 1u);
         s_last = (done == nblocks - 1);
@@ -467,9 +462,8 @@ __device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff,
         __threadfence();
         const Consts &K = *d.K;
         unsigned long long bl = atomicAdd(&d.clk->minl, 0ULL);
-        unsigned long long bd = atomicAdd(&d.clk->dtdiff, 0ULL);
         double minl = from_order_bits(bl);
-        double dt_diffusion = K.thermal ? from_order_bits(bd) : 1.7976931348623157e308;
+        double dt_diffusion = K.thermal ? 0.5 * minl * minl / K.therm_diff_max : 1.7976931348623157e308;
         double dt_maxwell = 1.7976931348623157e308;
         for (int i = 0; i < K.M.nmix; ++i) dt_maxwell = smin(dt_maxwell, K.M.mix[i].dt_maxwell);
         double dt_advection = 0.5 * minl / K.max_vbc_val;
@@ -488,7 +482,6 @@ __device__ void dt_reduce_and_finalize(const Dev &d, double minh, double dtdiff,
         d.clk->dt = dt;
         if (!(dt > 0)) atomicOr(&d.clk->status, 0x1u);
         d.clk->minl = ~0ULL;
-        d.clk->dtdiff = ~0ULL;
         d.clk->blocks_done = 0;
     }
 }
@@ -939,14 +932,13 @@ __global__ void k_dt(Dev d)
 {
     int e = gtid();
     bool live = e < d.nelem;
-    double minh = 0, dtd = 0;
+    double minh = 0;
     if (live) {
         double X[4][3];
         load_xyz4(d, d.conn[e], X);
         minh = min_height(X, d.vol[e]);
-        dtd = 0.5 * minh * minh / d.K->therm_diff_max;
     }
-    dt_reduce_and_finalize(d, minh, dtd, live, gridDim.x);
+    dt_reduce_and_finalize(d, minh, live, gridDim.x);
 }
 
 // ic.cxx:100-131
@@ -1204,7 +1196,7 @@ __global__ void __launch_bounds__(128, 6) k_fe_a(Dev d, int e0, unsigned nblocks
     const bool dt_step = (K.fixed_dt == 0) && (d.clk->steps % 10 == 0);
     if (e == 0) d.clk->mass_valid = 0;
     bool live = e < d.nelem;
-    double minh = 0, dtd = 0;
+    double minh = 0;
     if (live) {
         const size_t E = d.nelem;
         int4 c = d.conn[e];
@@ -1221,7 +1213,6 @@ __global__ void __launch_bounds__(128, 6) k_fe_a(Dev d, int e0, unsigned nblocks
         // before the rotation's registers are needed (geometry.cxx:280-300)
         if (dt_step) {
             minh = min_height(X, vol, r1, r3);
-            dtd = 0.5 * minh * minh / K.therm_diff_max;
         }
         const Mix &x = K.M.mix[d.mix[e]];
         {
@@ -1248,7 +1239,7 @@ __global__ void __launch_bounds__(128, 6) k_fe_a(Dev d, int e0, unsigned nblocks
         }
         next_step_contrib_d(d, e, c, D, dx, dy, dz, vol);
     }
-    if (dt_step) dt_reduce_and_finalize(d, minh, dtd, live, nblocks);
+    if (dt_step) dt_reduce_and_finalize(d, minh, live, nblocks);
 }
 
 // nodal masses from the fused-pass contributions (used before a download)

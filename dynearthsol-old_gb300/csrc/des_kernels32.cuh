@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(128, 9) kf_fe_a(DevF d, int e0, unsigned nbloc
     const bool dt_step = (K.fixed_dt == 0) && (d.clk->steps % 10 == 0);
     if (e == 0) d.clk->mass_valid = 0;
     bool live = e < d.nelem;
-    double minh = 0, dtd = 0;
+    double minh = 0;
     if (live) {
         const size_t E = d.nelem;
         int4 c = d.conn[e];
@@ -705,7 +705,6 @@ __global__ void __launch_bounds__(128, 9) kf_fe_a(DevF d, int e0, unsigned nbloc
             // the reference's 3 V / (largest face area) (geometry.cxx:280-293)
             // from the cofactors: 6 V / max |c_i|
             minh = 6 * vol / sqrt(c2max);
-            dtd = 0.5 * minh * minh / K.therm_diff_max;
         }
     }
     if (dt_step) {
@@ -715,7 +714,7 @@ __global__ void __launch_bounds__(128, 9) kf_fe_a(DevF d, int e0, unsigned nbloc
         dd.mix = d.mix;
         dd.K = d.K;
         dd.clk = d.clk;
-        dt_reduce_and_finalize(dd, minh, dtd, live, nblocks);
+        dt_reduce_and_finalize(dd, minh, live, nblocks);
     }
 }
 
