@@ -181,6 +181,16 @@ __device__ __forceinline__ void store6(double *a, size_t E, int e, const double 
 
 // rheology.cxx:525-646 for one element; returns eigen flags (bit0 solved,
 // bit1 QL, bit2 QL failed)
+// the plastic branch of elasto_plastic (rheology.cxx:154-302), out of line:
+// few elements take it
+static __device__ __noinline__ int plastic_branch(const MatTable &M, const Mix &x, double pls, double &depls,
+                                                  double s[6])
+{
+    double amc, anphi, anpsi, hardn, ten_max;
+    plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
+    return plastic_return(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
+}
+
 __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double edv, double dt,
                                            double s[6], double es[6], double edot[6], double &pls,
                                            double &dpls, double &dpress)
@@ -219,11 +229,7 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
     case 5: { // elasto-plastic
         double depls = 0;
         elastic(x.bulkm, x.shearm, de, s);
-        if (!quick_elastic(M, x, pls, s)) {
-            double amc, anphi, anpsi, hardn, ten_max;
-            plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
-            flags = plastic_return(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, depls, s);
-        }
+        if (!quick_elastic(M, x, pls, s)) flags = plastic_branch(M, x, pls, depls, s);
         pls += depls;
         dpls = depls;
     } break;
@@ -240,11 +246,7 @@ __device__ __forceinline__ int stress_body(const Dev &d, int e, int4 c, double e
         double sp[6];
         for (int i = 0; i < 6; ++i) sp[i] = s[i];
         elastic(x.bulkm, x.shearm, de, sp);
-        if (!quick_elastic(M, x, pls, sp)) {
-            double amc, anphi, anpsi, hardn, ten_max;
-            plastic_props(M, x, pls, amc, anphi, anpsi, hardn, ten_max);
-            flags = plastic_return(x.bulkm, x.shearm, amc, anphi, anpsi, hardn, ten_max, depls, sp);
-        }
+        if (!quick_elastic(M, x, pls, sp)) flags = plastic_branch(M, x, pls, depls, sp);
         double spII = second_invariant2(sp);
         if (svII < spII) {
             for (int i = 0; i < 6; ++i) s[i] = sv[i];
@@ -1060,11 +1062,11 @@ constexpr int kRetRecord = 24;
 // dilation factor anpsi of the return
 
 // (over the elements from e0, a multiple of the block size).  Registers
-// bounded for 5 blocks of 128 per SM: the spills fall in the return map,
-// which few elements take; config 2's E-B 1.08 -> 0.93 ms, the yielding
-// workload's 1.61 -> 1.47 ms.
+// bounded for 8 blocks of 128 per SM, with the return map out of line
+// (plastic_branch): the spills fall there, where few elements go; config 2's
+// E-B 1.08 -> 0.86 ms, the yielding workload's 1.61 -> 1.42 ms.
 template <bool LOG>
-__global__ void __launch_bounds__(128, 5) k_fe_b_t(Dev d, int e0)
+__global__ void __launch_bounds__(128, 8) k_fe_b_t(Dev d, int e0)
 {
     int e = e0 + gtid();
     if (e == 0) d.clk->mass_valid = 1;
