@@ -590,15 +590,24 @@ __global__ void kf_fn_c(DevF d)
     const float dtf = (float)dt;
     float g[3] = {0.f, 0.f, 0.f};
     double h[3] = {0.0, 0.0, 0.0};
-    for (int q = d.sup_off[n]; q < d.sup_off[n + 1]; ++q) {
+    // the FP64 reference part and the FP32 part in two walks over the
+    // support list, each streaming its own arrays (one walk over both:
+    // 282 against 194 B per element read from DRAM, 0.46 against 0.35 ms
+    // on config 2)
+    const int q0 = d.sup_off[n], q1 = d.sup_off[n + 1];
+    for (int q = q0; q < q1; ++q) {
+        unsigned p = __ldg(d.sup_ent + q);
+        size_t e = p >> 2, i = p & 3u;
+        h[0] -= d.f0[(i)*E + e];
+        h[1] -= d.f0[(i + 4) * E + e];
+        h[2] -= d.f0[(i + 8) * E + e];
+    }
+    for (int q = q0; q < q1; ++q) {
         unsigned p = __ldg(d.sup_ent + q);
         size_t e = p >> 2, i = p & 3u;
         g[0] -= d.tmp[(i)*E + e];
         g[1] -= d.tmp[(i + 4) * E + e];
         g[2] -= d.tmp[(i + 8) * E + e];
-        h[0] -= d.f0[(i)*E + e];
-        h[1] -= d.f0[(i + 4) * E + e];
-        h[2] -= d.f0[(i + 8) * E + e];
     }
     // the boundary tractions balance the FP64 reference part: FP64 as well
     stress_bc_node(K, d.bf, n, d.bcflag[n], d.z[n], d.z0[n], h);
