@@ -17,6 +17,7 @@ speed against the restatement, measured there on the same threads
 (oracle/ref_speed.json), is reported beside the number.
 """
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -209,12 +210,18 @@ def e2e_rate(dev, mesh, steps, barrier, world):
         dev.step_host(host, 1, mask)
     barrier()
     per_step = []
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        t1 = time.perf_counter()
-        dev.step_host(host, 1, mask)
-        per_step.append(time.perf_counter() - t1)
-    e2e_s = time.perf_counter() - t0
+    # no garbage collection inside the timed host loop (as timeit does)
+    gc.collect()
+    gc.disable()
+    try:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            t1 = time.perf_counter()
+            dev.step_host(host, 1, mask)
+            per_step.append(time.perf_counter() - t1)
+        e2e_s = time.perf_counter() - t0
+    finally:
+        gc.enable()
     D.unpin(host)
     e2e_rate.last_ms = {"min": 1e3 * min(per_step), "median": 1e3 * float(np.median(per_step)),
                         "max": 1e3 * max(per_step), "slowest_step": int(np.argmax(per_step))}
